@@ -1,0 +1,476 @@
+// capi.cpp -- extern "C" entry points of include/lbswim_c.h.
+//
+// Every entry point validates its arguments, converts exceptions into a status
+// code plus a thread-local message, and never exits the process (the
+// reference's CUDA_SAFE_CALL prints and calls exit(), cucall.h:5-14).
+#include <atomic>
+#include <cmath>
+#include <new>
+#include <string>
+
+#include "lbswim_internal.h"
+
+namespace lbswim {
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+void set_error(const std::string& m) { g_err = m; }
+void count_launches(unsigned long long n) { g_launches += n; }
+}  // namespace lbswim
+
+using namespace lbswim;
+
+#define API_BEGIN try {
+#define API_END                                 \
+  }                                             \
+  catch (const LbswimError& e) {                \
+    set_error(e.msg);                           \
+    return e.code;                              \
+  }                                             \
+  catch (const std::bad_alloc&) {               \
+    set_error("host allocation failed");        \
+    return LBSWIM_ENOMEM;                       \
+  }                                             \
+  catch (const std::exception& e) {             \
+    set_error(e.what());                        \
+    return LBSWIM_ECUDA;                        \
+  }                                             \
+  return LBSWIM_OK;
+
+#define REQUIRE(cond, msg)                                   \
+  do {                                                       \
+    if (!(cond)) throw LbswimError{LBSWIM_EINVAL, (msg)};    \
+  } while (0)
+
+static void check_lattice(const void* lat) { REQUIRE(lat, "lattice handle is NULL"); }
+
+extern "C" {
+
+const char* lbswim_last_error(void) { return g_err.c_str(); }
+const char* lbswim_version(void) { return "lbswim-gb300 1.0 (sm_103a)"; }
+
+int lbswim_kernel_launches(unsigned long long* count) {
+  if (!count) return LBSWIM_EINVAL;
+  *count = g_launches.load();
+  return LBSWIM_OK;
+}
+
+// ---- Lattice -------------------------------------------------------------------
+int lbswim_lattice_create(int nx, int ny, int nz, double tau_s, double tau_b, int precision,
+                          lbswim_lattice** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  REQUIRE(nx > 0 && ny > 0 && nz > 0, "lattice dimensions must be positive");
+  REQUIRE(nx <= 65535, "nx must be at most 65535");
+  REQUIRE(std::isfinite(tau_s) && std::isfinite(tau_b) && tau_s > -0.5 && tau_b > -0.5,
+          "relaxation times must be finite and > -1/2");
+  REQUIRE(precision >= LBSWIM_F64 && precision <= LBSWIM_F16, "unknown precision");
+  Lattice* L = new Lattice();
+  L->size[0] = nx;
+  L->size[1] = ny;
+  L->size[2] = nz;
+  L->n = (long long)nx * ny * nz;
+  L->precision = precision;
+  L->tau_s = tau_s;
+  L->tau_b = tau_b;
+  L->rho0 = precision == LBSWIM_F64 ? 0.0 : 1.0;
+  L->fused_tile = nz <= 16 ? 1 : 0;
+  fill_params(&L->params, tau_s, tau_b);
+  try {
+    lattice_alloc(L);
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+  } catch (...) {
+    lattice_free(L);
+    delete L;
+    throw;
+  }
+  *out = reinterpret_cast<lbswim_lattice*>(L);
+  API_END
+}
+
+int lbswim_lattice_destroy(lbswim_lattice* lat) {
+  API_BEGIN
+  if (!lat) return LBSWIM_OK;
+  Lattice* L = reinterpret_cast<Lattice*>(lat);
+  cudaStreamSynchronize(L->stream);
+  lattice_free(L);
+  delete L;
+  API_END
+}
+
+#define LAT(h) reinterpret_cast<Lattice*>(h)
+#define CLAT(h) reinterpret_cast<const Lattice*>(h)
+
+int lbswim_lattice_step(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  lattice_step(LAT(lat));
+  API_END
+}
+
+int lbswim_lattice_calc_hydro(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  lattice_calc_hydro(LAT(lat));
+  API_END
+}
+
+int lbswim_lattice_init_from_hydro(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  lattice_init_from_hydro(LAT(lat));
+  API_END
+}
+
+int lbswim_lattice_zero_force(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  // Deferred: the next consumer of the force either overwrites it (spreading)
+  // or treats it as zero; a read of the field clears the buffer first.
+  Lattice* L = LAT(lat);
+  L->force_zero_pending = true;
+  L->force_version++;
+  API_END
+}
+
+int lbswim_lattice_h2d(lbswim_lattice* lat, int field, const double* host) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
+  REQUIRE(host, "host buffer is NULL");
+  lattice_h2d(LAT(lat), field, host);
+  API_END
+}
+
+int lbswim_lattice_d2h(lbswim_lattice* lat, int field, double* host) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
+  REQUIRE(host, "host buffer is NULL");
+  lattice_d2h(LAT(lat), field, host);
+  API_END
+}
+
+int lbswim_lattice_get_params(const lbswim_lattice* lat, lbswim_lbparams* out) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  *out = CLAT(lat)->params;
+  API_END
+}
+
+int lbswim_lattice_get_addressing(const lbswim_lattice* lat, lbswim_addressing* out) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  const Lattice* L = CLAT(lat);
+  for (int a = 0; a < 3; ++a) out->size[a] = L->size[a];
+  out->strides[0] = L->size[1] * L->size[2];
+  out->strides[1] = L->size[2];
+  out->strides[2] = 1;
+  out->n = (int)std::min<long long>(L->n, 0x7fffffffLL);
+  API_END
+}
+
+int lbswim_lattice_get_time_step(const lbswim_lattice* lat, int* out) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  *out = CLAT(lat)->time_step;
+  API_END
+}
+
+int lbswim_lattice_set_time_step(lbswim_lattice* lat, int time_step) {
+  API_BEGIN
+  check_lattice(lat);
+  LAT(lat)->time_step = time_step;
+  API_END
+}
+
+int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  *out = CLAT(lat)->precision;
+  API_END
+}
+
+int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP)) == 0,
+          "unknown compat flag");
+  LAT(lat)->compat = flags;
+  API_END
+}
+
+int lbswim_lattice_set_stream(lbswim_lattice* lat, void* stream) {
+  API_BEGIN
+  check_lattice(lat);
+  Lattice* L = LAT(lat);
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  L->stream = (cudaStream_t)stream;
+  API_END
+}
+
+int lbswim_lattice_synchronize(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  LB_CUDA(cudaStreamSynchronize(LAT(lat)->stream));
+  API_END
+}
+
+int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, int* elem) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(ptr, "ptr is NULL");
+  REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
+  Lattice* L = const_cast<Lattice*>(CLAT(lat));
+  if (field == LBSWIM_FIELD_FORCE) lattice_materialise_force(L);
+  switch (field) {
+    case LBSWIM_FIELD_RHO: *ptr = L->rho; break;
+    case LBSWIM_FIELD_U: *ptr = L->u; break;
+    case LBSWIM_FIELD_FORCE: *ptr = L->force; break;
+    case LBSWIM_FIELD_FOLD: *ptr = L->f[L->cur]; break;
+    default: *ptr = L->f[L->cur ^ 1]; break;
+  }
+  if (elem) {
+    const bool is_f = field == LBSWIM_FIELD_FOLD || field == LBSWIM_FIELD_FNEW;
+    *elem = is_f ? elem_bytes(L->precision) : (L->precision == LBSWIM_F64 ? 8 : 4);
+  }
+  API_END
+}
+
+// ---- SwimmerArray ----------------------------------------------------------------
+static void check_common(const lbswim_common_params* p) {
+  REQUIRE(p, "CommonParams is NULL");
+  REQUIRE(std::isfinite(p->P) && std::isfinite(p->l) && std::isfinite(p->alpha) &&
+              std::isfinite(p->mobility),
+          "CommonParams fields must be finite");
+}
+
+int lbswim_swimmers_create(int n, const lbswim_common_params* p, lbswim_swimmers** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  REQUIRE(n >= 0, "swimmer count must be non-negative");
+  check_common(p);
+  Swimmers* W = new Swimmers();
+  W->n = n;
+  W->common = *p;
+  W->seed = p->seed;
+  W->step = 0;
+  try {
+    const size_t bytes = sizeof(double) * 3 * (size_t)(n > 0 ? n : 1);
+    LB_CUDA(cudaMalloc(&W->r, bytes));
+    LB_CUDA(cudaMalloc(&W->v, bytes));
+    LB_CUDA(cudaMalloc(&W->nv, bytes));
+    LB_CUDA(cudaMemset(W->r, 0, bytes));
+    LB_CUDA(cudaMemset(W->v, 0, bytes));
+    LB_CUDA(cudaMemset(W->nv, 0, bytes));
+  } catch (...) {
+    cudaFree(W->r);
+    cudaFree(W->v);
+    cudaFree(W->nv);
+    delete W;
+    throw;
+  }
+  *out = reinterpret_cast<lbswim_swimmers*>(W);
+  API_END
+}
+
+#define SW(h) reinterpret_cast<Swimmers*>(h)
+
+int lbswim_swimmers_destroy(lbswim_swimmers* sw) {
+  API_BEGIN
+  if (!sw) return LBSWIM_OK;
+  Swimmers* W = SW(sw);
+  cudaDeviceSynchronize();
+  cudaFree(W->r);
+  cudaFree(W->v);
+  cudaFree(W->nv);
+  delete W;
+  API_END
+}
+
+int lbswim_swimmers_set_common(lbswim_swimmers* sw, const lbswim_common_params* p) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  check_common(p);
+  SW(sw)->common = *p;
+  API_END
+}
+
+int lbswim_swimmers_get_common(const lbswim_swimmers* sw, lbswim_common_params* out) {
+  API_BEGIN
+  REQUIRE(sw && out, "NULL argument");
+  *out = reinterpret_cast<const Swimmers*>(sw)->common;
+  API_END
+}
+
+int lbswim_swimmers_get_num(const lbswim_swimmers* sw, int* out) {
+  API_BEGIN
+  REQUIRE(sw && out, "NULL argument");
+  *out = reinterpret_cast<const Swimmers*>(sw)->n;
+  API_END
+}
+
+int lbswim_swimmers_add_forces(lbswim_swimmers* sw, lbswim_lattice* lat) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  check_lattice(lat);
+  swimmers_add_forces(SW(sw), LAT(lat));
+  API_END
+}
+
+int lbswim_swimmers_move(lbswim_swimmers* sw, lbswim_lattice* lat) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  check_lattice(lat);
+  swimmers_move(SW(sw), LAT(lat));
+  API_END
+}
+
+static double* sw_field(Swimmers* W, int field) {
+  REQUIRE(field >= LBSWIM_SW_R && field <= LBSWIM_SW_N, "unknown swimmer field");
+  return field == LBSWIM_SW_R ? W->r : (field == LBSWIM_SW_V ? W->v : W->nv);
+}
+
+int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host) {
+  API_BEGIN
+  REQUIRE(sw && host, "NULL argument");
+  Swimmers* W = SW(sw);
+  LB_CUDA(cudaDeviceSynchronize());  // particle arrays are not bound to one stream
+  LB_CUDA(cudaMemcpy(sw_field(W, field), host, sizeof(double) * 3 * W->n, cudaMemcpyHostToDevice));
+  API_END
+}
+
+int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host) {
+  API_BEGIN
+  REQUIRE(sw && host, "NULL argument");
+  Swimmers* W = SW(sw);
+  LB_CUDA(cudaDeviceSynchronize());
+  LB_CUDA(cudaMemcpy(host, sw_field(W, field), sizeof(double) * 3 * W->n, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int lbswim_swimmers_get_rng(const lbswim_swimmers* sw, unsigned long long* seed,
+                            unsigned long long* step) {
+  API_BEGIN
+  REQUIRE(sw && seed && step, "NULL argument");
+  *seed = reinterpret_cast<const Swimmers*>(sw)->seed;
+  *step = reinterpret_cast<const Swimmers*>(sw)->step;
+  API_END
+}
+
+int lbswim_swimmers_set_rng(lbswim_swimmers* sw, unsigned long long seed, unsigned long long step) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  SW(sw)->seed = seed;
+  SW(sw)->step = step;
+  API_END
+}
+
+// ---- TracerArray -----------------------------------------------------------------
+int lbswim_tracers_create(int n, lbswim_tracers** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  REQUIRE(n >= 0, "tracer count must be non-negative");
+  Tracers* T = new Tracers();
+  T->n = n;
+  try {
+    const size_t bytes = sizeof(double) * 3 * (size_t)(n > 0 ? n : 1);
+    LB_CUDA(cudaMalloc(&T->r, bytes));
+    LB_CUDA(cudaMalloc(&T->s, bytes));
+    LB_CUDA(cudaMalloc(&T->v, bytes));
+    LB_CUDA(cudaMemset(T->r, 0, bytes));
+    LB_CUDA(cudaMemset(T->s, 0, bytes));
+    LB_CUDA(cudaMemset(T->v, 0, bytes));
+  } catch (...) {
+    cudaFree(T->r);
+    cudaFree(T->s);
+    cudaFree(T->v);
+    delete T;
+    throw;
+  }
+  *out = reinterpret_cast<lbswim_tracers*>(T);
+  API_END
+}
+
+#define TR(h) reinterpret_cast<Tracers*>(h)
+
+int lbswim_tracers_destroy(lbswim_tracers* tr) {
+  API_BEGIN
+  if (!tr) return LBSWIM_OK;
+  Tracers* T = TR(tr);
+  cudaDeviceSynchronize();
+  cudaFree(T->r);
+  cudaFree(T->s);
+  cudaFree(T->v);
+  delete T;
+  API_END
+}
+
+int lbswim_tracers_get_num(const lbswim_tracers* tr, int* out) {
+  API_BEGIN
+  REQUIRE(tr && out, "NULL argument");
+  *out = reinterpret_cast<const Tracers*>(tr)->n;
+  API_END
+}
+
+int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat) {
+  API_BEGIN
+  REQUIRE(tr, "tracers handle is NULL");
+  check_lattice(lat);
+  tracers_move(TR(tr), LAT(lat));
+  API_END
+}
+
+static double* tr_field(Tracers* T, int field) {
+  REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
+  return field == LBSWIM_TR_R ? T->r : (field == LBSWIM_TR_S ? T->s : T->v);
+}
+
+int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host) {
+  API_BEGIN
+  REQUIRE(tr && host, "NULL argument");
+  Tracers* T = TR(tr);
+  LB_CUDA(cudaDeviceSynchronize());
+  LB_CUDA(cudaMemcpy(tr_field(T, field), host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+  API_END
+}
+
+int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host) {
+  API_BEGIN
+  REQUIRE(tr && host, "NULL argument");
+  Tracers* T = TR(tr);
+  LB_CUDA(cudaDeviceSynchronize());
+  LB_CUDA(cudaMemcpy(host, tr_field(T, field), sizeof(double) * 3 * T->n, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+// ---- System.Step -----------------------------------------------------------------
+int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, int n_swimmers,
+                       lbswim_tracers* const* tracers, int n_tracers, int nsteps) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(n_swimmers >= 0 && n_tracers >= 0 && nsteps >= 0, "counts must be non-negative");
+  REQUIRE(n_swimmers == 0 || swimmers, "swimmer list is NULL");
+  REQUIRE(n_tracers == 0 || tracers, "tracer list is NULL");
+  for (int i = 0; i < n_swimmers; ++i) REQUIRE(swimmers[i], "swimmer handle is NULL");
+  for (int i = 0; i < n_tracers; ++i) REQUIRE(tracers[i], "tracer handle is NULL");
+  Lattice* L = LAT(lat);
+  for (int t = 0; t < nsteps; ++t) {
+    L->force_zero_pending = true;  // ZeroForce
+    L->force_version++;
+    for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
+    lattice_step(L);
+    lattice_calc_hydro(L);
+    for (int i = 0; i < n_swimmers; ++i) swimmers_move(SW(swimmers[i]), L);
+    for (int i = 0; i < n_tracers; ++i) tracers_move(TR(tracers[i]), L);
+  }
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,644 @@
+// lattice.cu -- D3Q15 MRT lattice-Boltzmann kernels and Lattice operations.
+//
+// Two methods share the Lattice object:
+//  * FP64 (LBSWIM_F64): the reference's method, one kernel per reference op.
+//    Step is collide + push-stream (lb.cu:72-218) with Z, the contiguous axis,
+//    across the warp; CalcHydro is its own kernel (lb.cu:250-295).
+//  * FP32 / BF16 / FP16: one fused kernel per Step that reads f(t) and F(t),
+//    collides a tile plus a one-site halo, streams inside shared memory and
+//    writes f(t+1) together with rho(t+1), u(t+1).  CalcHydro then only has to
+//    publish those fields (pointer swap) when nothing changed since the Step.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "lbswim_device.cuh"
+#include "lbswim_internal.h"
+
+namespace lbswim {
+
+// ---------------------------------------------------------------------------
+// LBParams tables (reference d3q15.c:2-186), built from their definitions.
+// ---------------------------------------------------------------------------
+static const int kC[15][3] = {{0, 0, 0},   {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                              {0, 0, 1},   {0, 0, -1},  {1, 1, 1},  {1, 1, -1}, {1, -1, 1},
+                              {1, -1, -1}, {-1, 1, 1},  {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}};
+
+// Mode m on velocity c as num/den (den 1 or 3); rows follow d3q15.h:13-28.
+static void mode_rational(int m, const int* c, long& num, long& den) {
+  const int x = c[0], y = c[1], z = c[2], c2 = x * x + y * y + z * z;
+  const int chi1 = c2 == 1 ? 1 : -2;
+  den = 1;
+  switch (m) {
+    case 0: num = 1; break;
+    case 1: num = x; break;
+    case 2: num = y; break;
+    case 3: num = z; break;
+    case 4: num = 3 * x * x - 1; den = 3; break;
+    case 5: num = x * y; break;
+    case 6: num = x * z; break;
+    case 7: num = 3 * y * y - 1; den = 3; break;
+    case 8: num = y * z; break;
+    case 9: num = 3 * z * z - 1; den = 3; break;
+    case 10: num = chi1; break;
+    case 11: num = chi1 * x; break;
+    case 12: num = chi1 * y; break;
+    case 13: num = chi1 * z; break;
+    default: num = x * y * z; break;
+  }
+}
+
+static long gcd_l(long a, long b) {
+  a = a < 0 ? -a : a;
+  b = b < 0 ? -b : b;
+  while (b) {
+    const long t = a % b;
+    a = b;
+    b = t;
+  }
+  return a ? a : 1;
+}
+
+static double ratio(long num, long den) {
+  if (den < 0) {
+    num = -num;
+    den = -den;
+  }
+  const long g = gcd_l(num, den);
+  num /= g;
+  den /= g;
+  return den == 1 ? (double)num : (double)num / (double)den;
+}
+
+void fill_params(lbswim_lbparams* P, double tau_s, double tau_b) {
+  std::memset(P, 0, sizeof(*P));
+  P->cs2 = 1. / 3.;
+  P->tau_s = tau_s;
+  P->tau_b = tau_b;
+  long wn[15], wd[15];
+  for (int p = 0; p < 15; ++p) {
+    const int c2 = kC[p][0] * kC[p][0] + kC[p][1] * kC[p][1] + kC[p][2] * kC[p][2];
+    wn[p] = c2 == 0 ? 2 : 1;
+    wd[p] = c2 == 0 ? 9 : (c2 == 1 ? 9 : 72);
+    P->w[p] = ratio(wn[p], wd[p]);
+    for (int a = 0; a < 3; ++a) {
+      P->ci[p][a] = kC[p][a];
+      P->xi[p][a] = kC[p][a];
+      for (int b = 0; b < 3; ++b) P->Q[p][a][b] = ratio(3 * kC[p][a] * kC[p][b] - (a == b), 3);
+    }
+    for (int q = 0; q < 15; ++q)
+      if (kC[q][0] == -kC[p][0] && kC[q][1] == -kC[p][1] && kC[q][2] == -kC[p][2])
+        P->complement[p] = q;
+  }
+  for (int m = 0; m < 15; ++m) {
+    long sn = 0, sd = 1;  // sum_p w_p mm[m][p]^2
+    for (int p = 0; p < 15; ++p) {
+      long mn, md;
+      mode_rational(m, kC[p], mn, md);
+      const long tn = wn[p] * mn * mn, td = wd[p] * md * md;
+      const long nn = sn * td + tn * sd, nd = sd * td, g = gcd_l(nn, nd);
+      sn = nn / g;
+      sd = nd / g;
+    }
+    P->norms[m] = ratio(sd, sn);
+    for (int p = 0; p < 15; ++p) {
+      long mn, md;
+      mode_rational(m, kC[p], mn, md);
+      P->mm[m][p] = ratio(mn, md);
+      P->mmi[p][m] = mn == 0 ? 0.0 : ratio(wn[p] * mn * sd, wd[p] * md * sn);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void load_force(const T* F, long long N, long long s, T& fx, T& fy,
+                                           T& fz) {
+  if (F) {
+    fx = F[s];
+    fy = F[N + s];
+    fz = F[2 * N + s];
+  } else {
+    fx = fy = fz = T(0);
+  }
+}
+
+// FP64 collide + push-stream, lb.cu:72-218.  blockDim = (32, 8); grid.z = x.
+__global__ void __launch_bounds__(256) k_step_push_f64(const double* __restrict__ f,
+                                                       const double* __restrict__ F,
+                                                       double* __restrict__ fn, int nx, int ny,
+                                                       int nz, long long N, Relax<double> k) {
+  const int z = blockIdx.x * 32 + threadIdx.x;
+  const int y = blockIdx.y * 8 + threadIdx.y;
+  const int x = blockIdx.z;
+  if (z >= nz || y >= ny) return;
+  const long long nynz = (long long)ny * nz;
+  const long long s = x * nynz + (long long)y * nz + z;
+  double d[15];
+#pragma unroll
+  for (int p = 0; p < 15; ++p) d[p] = f[p * N + s];
+  double fx, fy, fz;
+  load_force(F, N, s, fx, fy, fz);
+  collide(d, fx, fy, fz, 0.0, k, d);
+  const int xm = wrap_once(x - 1, nx), xp = wrap_once(x + 1, nx);
+  const int ym = wrap_once(y - 1, ny), yp = wrap_once(y + 1, ny);
+  const int zm = wrap_once(z - 1, nz), zp = wrap_once(z + 1, nz);
+#pragma unroll
+  for (int p = 0; p < 15; ++p) {
+    const int dx = cx_of(p), dy = cy_of(p), dz = cz_of(p);
+    const long long X = dx > 0 ? xp : (dx < 0 ? xm : x);
+    const long long Y = dy > 0 ? yp : (dy < 0 ? ym : y);
+    const long long Z = dz > 0 ? zp : (dz < 0 ? zm : z);
+    fn[p * N + X * nynz + Y * nz + Z] = d[p];
+  }
+}
+
+// rho, u from the stored distributions and the force, lb.cu:250-295.
+template <class S, class H>
+__global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H* __restrict__ rho,
+                             H* __restrict__ u, long long N, H rho0) {
+  using T = H;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
+       s += (long long)gridDim.x * blockDim.x) {
+    T d[15];
+#pragma unroll
+    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((T)Store<S>::ld(f + p * N + s), p);
+    T R, jx, jy, jz;
+    hydro_moments(d, R, jx, jy, jz);
+    T fx, fy, fz;
+    load_force(F, N, s, fx, fy, fz);
+    const T r = rho0 + R;
+    rho[s] = r;
+    u[s] = (jx + T(0.5) * fx) / r;
+    u[N + s] = (jy + T(0.5) * fy) / r;
+    u[2 * N + s] = (jz + T(0.5) * fz) / r;
+  }
+}
+
+// Equilibrium from rho, u, lb.cu:314-371 (compat_sxz reproduces lb.cu:356).
+template <class S, class H>
+__global__ void k_init_from_hydro(const H* __restrict__ rho, const H* __restrict__ u,
+                                  S* __restrict__ f, long long N, double rho0, int compat_sxz) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
+       s += (long long)gridDim.x * blockDim.x) {
+    const double r = rho[s], ux = u[s], uy = u[N + s], uz = u[2 * N + s];
+    double out[15];
+    project<double>(r - rho0, r * ux, r * uy, r * uz, r * ux * ux, r * uy * uy, r * uz * uz,
+                    r * ux * uy, compat_sxz ? r * ux * uy : r * ux * uz, r * uy * uz, out);
+#pragma unroll
+    for (int p = 0; p < 15; ++p) Store<S>::st(f + p * N + s, (S)stored_from_dev<S>(out[p], p));
+  }
+}
+
+// Host FP64 <-> device storage conversions for H2D / D2H of fOld and fNew.
+template <class S>
+__global__ void k_f_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long off,
+                             long long cnt, long long N, double rho0) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long e = off + i;
+    const int p = (int)(e / N);
+    const double d = src[i] - w_of(p) * rho0;
+    Store<S>::st(dst + e, (S)stored_from_dev<S>(d, p));
+  }
+}
+template <class S>
+__global__ void k_f_to_f64(const S* __restrict__ src, double* __restrict__ dst, long long off,
+                           long long cnt, long long N, double rho0) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long e = off + i;
+    const int p = (int)(e / N);
+    dst[i] = dev_from_stored<S>((double)Store<S>::ld(src + e), p) + w_of(p) * rho0;
+  }
+}
+__global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long cnt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+__global__ void k_f32_to_f64(const float* __restrict__ src, double* __restrict__ dst, long long cnt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+// ---------------------------------------------------------------------------
+// Fused collide + stream + hydro kernel (FP32 arithmetic).
+//
+// A CTA owns a TY x TZ cross-section (y, z) of FUSED_LX consecutive x planes
+// and marches along x.  For each plane it collides the cross-section plus a
+// one-site ring (TY*TZ interior threads + up to 96 ring threads) and parks
+// the post-collision values in a 4-slot ring buffer of shared memory.  Once
+// the planes x-1, x, x+1 are in the ring, each interior thread pulls its 15
+// post-stream populations for plane x, computes rho and u with the same force
+// used in the collision (lb.cu:286-293) and writes f(t+1), rho, u.  The next
+// plane's loads are issued before the current plane is collided.
+// ---------------------------------------------------------------------------
+constexpr int FUSED_LX = 32;
+constexpr int FUSED_RING_THREADS = 96;
+
+struct FusedArgs {
+  const void* f_old;
+  void* f_new;
+  const float* force;  // null: zero force
+  float* rho;
+  float* u;
+  int nx, ny, nz;
+  long long n;
+  float rho0;
+  Relax<float> k;
+};
+
+template <int TZ, int TY>
+constexpr int fused_smem_bytes() {
+  return 4 * 15 * (TY + 2) * (TZ + 2) * (int)sizeof(float);
+}
+
+template <class S, int TZ, int TY>
+__global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
+  constexpr int NI = TY * TZ;
+  constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ, SLOT = 15 * PLANE;
+  extern __shared__ float sm[];
+  const int tid = threadIdx.x;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * FUSED_LX;
+  const int ez = min(TZ, nz - z0), ey = min(TY, ny - y0), ex = min(FUSED_LX, nx - x0);
+
+  int ly = 0, lz = 0;
+  bool active = false, interior = false;
+  if (tid < NI) {
+    ly = tid / TZ + 1;
+    lz = tid % TZ + 1;
+    interior = active = (ly <= ey) && (lz <= ez);
+  } else {
+    int h = tid - NI;
+    const int rowN = ez + 2;
+    if (h < 2 * rowN) {
+      ly = h < rowN ? 0 : ey + 1;
+      lz = h < rowN ? h : h - rowN;
+      active = true;
+    } else {
+      h -= 2 * rowN;
+      if (h < 2 * ey) {
+        ly = 1 + (h >> 1);
+        lz = (h & 1) ? ez + 1 : 0;
+        active = true;
+      }
+    }
+  }
+  const int gy = wrap_once(y0 + ly - 1, ny), gz = wrap_once(z0 + lz - 1, nz);
+  const long long nynz = (long long)ny * nz, N = a.n;
+  const long long yz = (long long)gy * nz + gz;
+  const S* __restrict__ fo = (const S*)a.f_old;
+  const float* __restrict__ F = a.force;
+
+  float pre[18];
+  auto load = [&](int gx) {
+    const long long s = gx * nynz + yz;
+#pragma unroll
+    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(fo + p * N + s);
+    if (F) {
+      pre[15] = F[s];
+      pre[16] = F[N + s];
+      pre[17] = F[2 * N + s];
+    } else {
+      pre[15] = pre[16] = pre[17] = 0.f;
+    }
+  };
+  if (active) load(wrap_once(x0 - 1, nx));
+
+  float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f;
+  const int my = ly * HZ + lz;
+  for (int k = 0; k < ex + 2; ++k) {
+    float cur[18];
+#pragma unroll
+    for (int i = 0; i < 18; ++i) cur[i] = pre[i];
+    if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
+    if (active) {
+      float d[15];
+#pragma unroll
+      for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>(cur[p], p);
+      collide(d, cur[15], cur[16], cur[17], a.rho0, a.k, d);
+      float* slot = sm + (k & 3) * SLOT + my;
+#pragma unroll
+      for (int p = 0; p < 15; ++p) slot[p * PLANE] = d[p];
+    }
+    __syncthreads();
+    if (k >= 2 && interior) {
+      const long long s = (long long)(x0 + k - 2) * nynz + yz;
+      const float* sm_m = sm + ((k - 2) & 3) * SLOT + my;  // plane x-1: c_x = +1
+      const float* sm_0 = sm + ((k - 1) & 3) * SLOT + my;  // plane x:   c_x = 0
+      const float* sm_p = sm + (k & 3) * SLOT + my;        // plane x+1: c_x = -1
+      float g[15];
+#pragma unroll
+      for (int p = 0; p < 15; ++p) {
+        const int off = p * PLANE - cy_of(p) * HZ - cz_of(p);
+        g[p] = cx_of(p) > 0 ? sm_m[off] : (cx_of(p) < 0 ? sm_p[off] : sm_0[off]);
+      }
+      float R, jx, jy, jz;
+      hydro_moments(g, R, jx, jy, jz);
+      S* __restrict__ fn = (S*)a.f_new;
+#pragma unroll
+      for (int p = 0; p < 15; ++p) Store<S>::st(fn + p * N + s, stored_from_dev<S>(g[p], p));
+      const float rho = a.rho0 + R;
+      const float inv = 1.0f / rho;
+      a.rho[s] = rho;
+      a.u[s] = (jx + 0.5f * Fp0) * inv;
+      a.u[N + s] = (jy + 0.5f * Fp1) * inv;
+      a.u[2 * N + s] = (jz + 0.5f * Fp2) * inv;
+    }
+    Fp0 = cur[15];
+    Fp1 = cur[16];
+    Fp2 = cur[17];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  return (int)std::max(1LL, std::min(g, 152LL * 16));
+}
+
+static void* dmalloc(size_t bytes) {
+  void* p = nullptr;
+  LB_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+  return p;
+}
+
+void lattice_alloc(Lattice* L) {
+  const long long N = L->n;
+  const size_t fe = elem_bytes(L->precision);
+  const size_t he = L->precision == LBSWIM_F64 ? 8 : 4;
+  L->f[0] = dmalloc(15 * N * fe);
+  L->f[1] = dmalloc(15 * N * fe);
+  L->rho = dmalloc(N * he);
+  L->u = dmalloc(3 * N * he);
+  L->force = dmalloc(3 * N * he);
+  if (L->precision != LBSWIM_F64) {
+    L->rho_shadow = dmalloc(N * he);
+    L->u_shadow = dmalloc(3 * N * he);
+  }
+  // Contents start at zero so that reading a field before setting it is defined.
+  LB_CUDA(cudaMemsetAsync(L->rho, 0, N * he, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->u, 0, 3 * N * he, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * N * he, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->f[0], 0, 15 * N * fe, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->f[1], 0, 15 * N * fe, L->stream));
+}
+
+void lattice_free(Lattice* L) {
+  void* ptrs[] = {L->f[0], L->f[1], L->rho, L->u, L->rho_shadow, L->u_shadow, L->force,
+                  L->staging, L->spread.bin_count, L->spread.bin_start, L->spread.scan_tmp,
+                  L->spread.order, L->spread.ends};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+static double* staging(Lattice* L, size_t elems) {
+  if (L->staging_elems < elems) {
+    if (L->staging) {
+      LB_CUDA(cudaStreamSynchronize(L->stream));
+      LB_CUDA(cudaFree(L->staging));
+      L->staging = nullptr;
+      L->staging_elems = 0;
+    }
+    L->staging = (double*)dmalloc(elems * sizeof(double));
+    L->staging_elems = elems;
+  }
+  return L->staging;
+}
+
+void lattice_zero_force_now(Lattice* L) {
+  const size_t he = L->precision == LBSWIM_F64 ? 8 : 4;
+  LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * L->n * he, L->stream));
+  L->force_zero_pending = false;
+}
+
+void lattice_materialise_force(Lattice* L) {
+  if (L->force_zero_pending) lattice_zero_force_now(L);
+}
+
+template <class S>
+static void init_from_hydro_t(Lattice* L) {
+  const long long N = L->n;
+  const int compat = (L->compat & LBSWIM_COMPAT_INIT_SXZ) ? 1 : 0;
+  if (L->precision == LBSWIM_F64)
+    k_init_from_hydro<S, double><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const double*)L->rho, (const double*)L->u, (S*)L->f[L->cur], N, 0.0, compat);
+  else
+    k_init_from_hydro<S, float><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const float*)L->rho, (const float*)L->u, (S*)L->f[L->cur], N, L->rho0, compat);
+  LB_CHECK_LAUNCH(1);
+}
+
+void lattice_init_from_hydro(Lattice* L) {
+  switch (L->precision) {
+    case LBSWIM_F64: init_from_hydro_t<double>(L); break;
+    case LBSWIM_F32: init_from_hydro_t<float>(L); break;
+    case LBSWIM_BF16: init_from_hydro_t<__nv_bfloat16>(L); break;
+    default: init_from_hydro_t<__half>(L); break;
+  }
+  L->f_version++;
+}
+
+template <class S, int TZ, int TY>
+static void launch_fused(Lattice* L, const FusedArgs& a) {
+  constexpr int smem = fused_smem_bytes<TZ, TY>();
+  static bool configured = false;  // per template instance, per process
+  if (!configured) {
+    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  dim3 grid((a.nz + TZ - 1) / TZ, (a.ny + TY - 1) / TY, (a.nx + FUSED_LX - 1) / FUSED_LX);
+  k_fused_step<S, TZ, TY><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
+  LB_CHECK_LAUNCH(1);
+}
+
+template <class S>
+static void fused_step_t(Lattice* L) {
+  FusedArgs a;
+  a.f_old = L->f[L->cur];
+  a.f_new = L->f[L->cur ^ 1];
+  a.force = L->force_zero_pending ? nullptr : (const float*)L->force;
+  a.rho = (float*)L->rho_shadow;
+  a.u = (float*)L->u_shadow;
+  a.nx = L->size[0];
+  a.ny = L->size[1];
+  a.nz = L->size[2];
+  a.n = L->n;
+  a.rho0 = (float)L->rho0;
+  a.k = make_relax<float>(L->tau_s, L->tau_b);
+  if (L->fused_tile == 1)
+    launch_fused<S, 16, 16>(L, a);
+  else
+    launch_fused<S, 32, 8>(L, a);
+}
+
+void lattice_step(Lattice* L) {
+  const int nx = L->size[0], ny = L->size[1], nz = L->size[2];
+  if (L->precision == LBSWIM_F64) {
+    dim3 grid((nz + 31) / 32, (ny + 7) / 8, nx);
+    k_step_push_f64<<<grid, dim3(32, 8), 0, L->stream>>>(
+        (const double*)L->f[L->cur], L->force_zero_pending ? nullptr : (const double*)L->force,
+        (double*)L->f[L->cur ^ 1], nx, ny, nz, L->n, make_relax<double>(L->tau_s, L->tau_b));
+    LB_CHECK_LAUNCH(1);
+  } else {
+    switch (L->precision) {
+      case LBSWIM_F32: fused_step_t<float>(L); break;
+      case LBSWIM_BF16: fused_step_t<__nv_bfloat16>(L); break;
+      default: fused_step_t<__half>(L); break;
+    }
+  }
+  L->cur ^= 1;
+  L->f_version++;
+  if (L->precision != LBSWIM_F64) {
+    L->shadow_f_version = L->f_version;
+    L->shadow_force_version = L->force_version;
+  }
+  L->time_step++;
+  if (L->compat & LBSWIM_COMPAT_SYNC_STEP) LB_CUDA(cudaStreamSynchronize(L->stream));
+}
+
+template <class S, class H>
+static void calc_hydro_t(Lattice* L) {
+  const long long N = L->n;
+  k_calc_hydro<S, H><<<grid_for(N, 256), 256, 0, L->stream>>>(
+      (const S*)L->f[L->cur], L->force_zero_pending ? nullptr : (const H*)L->force, (H*)L->rho,
+      (H*)L->u, N, (H)L->rho0);
+  LB_CHECK_LAUNCH(1);
+}
+
+void lattice_calc_hydro(Lattice* L) {
+  if (L->precision != LBSWIM_F64 && L->shadow_f_version == L->f_version &&
+      L->shadow_force_version == L->force_version) {
+    // The last Step already produced rho, u for this fOld and this force.
+    std::swap(L->rho, L->rho_shadow);
+    std::swap(L->u, L->u_shadow);
+    L->shadow_f_version = 0;
+    return;
+  }
+  switch (L->precision) {
+    case LBSWIM_F64: calc_hydro_t<double, double>(L); break;
+    case LBSWIM_F32: calc_hydro_t<float, float>(L); break;
+    case LBSWIM_BF16: calc_hydro_t<__nv_bfloat16, float>(L); break;
+    default: calc_hydro_t<__half, float>(L); break;
+  }
+}
+
+static long long field_count(const Lattice* L, int field) {
+  static const int mult[5] = {1, 3, 3, 15, 15};
+  return mult[field] * L->n;
+}
+
+template <class S>
+static void f_h2d_t(Lattice* L, void* dst, const double* host) {
+  const long long total = 15 * L->n;
+  const long long chunk = std::min<long long>(total, 1LL << 24);
+  double* st = staging(L, chunk);
+  for (long long off = 0; off < total; off += chunk) {
+    const long long cnt = std::min(chunk, total - off);
+    LB_CUDA(cudaMemcpyAsync(st, host + off, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                            L->stream));
+    k_f_from_f64<S><<<grid_for(cnt, 256), 256, 0, L->stream>>>(st, (S*)dst, off, cnt, L->n,
+                                                                L->rho0);
+    LB_CHECK_LAUNCH(1);
+  }
+}
+
+template <class S>
+static void f_d2h_t(Lattice* L, const void* src, double* host) {
+  const long long total = 15 * L->n;
+  const long long chunk = std::min<long long>(total, 1LL << 24);
+  double* st = staging(L, chunk);
+  for (long long off = 0; off < total; off += chunk) {
+    const long long cnt = std::min(chunk, total - off);
+    k_f_to_f64<S><<<grid_for(cnt, 256), 256, 0, L->stream>>>((const S*)src, st, off, cnt, L->n,
+                                                              L->rho0);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaMemcpyAsync(host + off, st, cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                            L->stream));
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+  }
+}
+
+static void* field_ptr(Lattice* L, int field) {
+  switch (field) {
+    case LBSWIM_FIELD_RHO: return L->rho;
+    case LBSWIM_FIELD_U: return L->u;
+    case LBSWIM_FIELD_FORCE: return L->force;
+    case LBSWIM_FIELD_FOLD: return L->f[L->cur];
+    default: return L->f[L->cur ^ 1];
+  }
+}
+
+void lattice_h2d(Lattice* L, int field, const double* host) {
+  const long long cnt = field_count(L, field);
+  void* dst = field_ptr(L, field);
+  if (field == LBSWIM_FIELD_FORCE) {
+    L->force_zero_pending = false;
+    L->force_version++;
+  }
+  if (field == LBSWIM_FIELD_FOLD) L->f_version++;
+  if (L->precision == LBSWIM_F64) {
+    LB_CUDA(cudaMemcpyAsync(dst, host, cnt * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    return;
+  }
+  if (field == LBSWIM_FIELD_FOLD || field == LBSWIM_FIELD_FNEW) {
+    switch (L->precision) {
+      case LBSWIM_F32: f_h2d_t<float>(L, dst, host); break;
+      case LBSWIM_BF16: f_h2d_t<__nv_bfloat16>(L, dst, host); break;
+      default: f_h2d_t<__half>(L, dst, host); break;
+    }
+  } else {
+    const long long chunk = std::min<long long>(cnt, 1LL << 24);
+    double* st = staging(L, chunk);
+    for (long long off = 0; off < cnt; off += chunk) {
+      const long long c = std::min(chunk, cnt - off);
+      LB_CUDA(cudaMemcpyAsync(st, host + off, c * sizeof(double), cudaMemcpyHostToDevice,
+                              L->stream));
+      k_f64_to_f32<<<grid_for(c, 256), 256, 0, L->stream>>>(st, (float*)dst + off, c);
+      LB_CHECK_LAUNCH(1);
+    }
+  }
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+}
+
+void lattice_d2h(Lattice* L, int field, double* host) {
+  if (field == LBSWIM_FIELD_FORCE) lattice_materialise_force(L);
+  const long long cnt = field_count(L, field);
+  const void* src = field_ptr(L, field);
+  if (L->precision == LBSWIM_F64) {
+    LB_CUDA(cudaMemcpyAsync(host, src, cnt * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    return;
+  }
+  if (field == LBSWIM_FIELD_FOLD || field == LBSWIM_FIELD_FNEW) {
+    switch (L->precision) {
+      case LBSWIM_F32: f_d2h_t<float>(L, src, host); break;
+      case LBSWIM_BF16: f_d2h_t<__nv_bfloat16>(L, src, host); break;
+      default: f_d2h_t<__half>(L, src, host); break;
+    }
+    return;
+  }
+  const long long chunk = std::min<long long>(cnt, 1LL << 24);
+  double* st = staging(L, chunk);
+  for (long long off = 0; off < cnt; off += chunk) {
+    const long long c = std::min(chunk, cnt - off);
+    k_f32_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>((const float*)src + off, st, c);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaMemcpyAsync(host + off, st, c * sizeof(double), cudaMemcpyDeviceToHost,
+                            L->stream));
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+  }
+}
+
+}  // namespace lbswim

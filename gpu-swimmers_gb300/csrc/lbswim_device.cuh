@@ -1,0 +1,273 @@
+// lbswim_device.cuh -- device-side building blocks shared by the kernels.
+//
+// D3Q15 velocity ordering (reference d3q15.c:41-55): rest, +-x, +-y, +-z, then
+// the eight corners (x, y, z) = +++, ++-, +-+, +--, -++, -+-, --+, --- .
+// The distributions of a site are reduced to the ten moments the collision
+// uses (rho, j, S) with a 3-stage butterfly over the corners, and rebuilt from
+// them with the inverse butterfly.  This is the reference's dense 15x15
+// transform (lb.cu:114-119, 198-203) with the zero entries and the zeroed
+// ghost modes (lb.cu:191-195) taken out: f_p = w_p (rho + 3 c_p.j + 9/2 Q_p:S).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbswim {
+
+__host__ __device__ constexpr int cx_of(int p) {
+  return p == 1 ? 1 : p == 2 ? -1 : (p >= 7 && p <= 10) ? 1 : (p >= 11) ? -1 : 0;
+}
+__host__ __device__ constexpr int cy_of(int p) {
+  return p == 3 ? 1 : p == 4 ? -1 : (p == 7 || p == 8 || p == 11 || p == 12) ? 1
+         : (p == 9 || p == 10 || p == 13 || p == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int cz_of(int p) {
+  return p == 5 ? 1 : p == 6 ? -1 : (p >= 7 && (p & 1)) ? 1 : (p >= 8 && !(p & 1)) ? -1 : 0;
+}
+__host__ __device__ constexpr double w_of(int p) {
+  return p == 0 ? 2.0 / 9.0 : p <= 6 ? 1.0 / 9.0 : 1.0 / 72.0;
+}
+
+// Relaxation constants of one lattice (lb.cu:105-108, 165, 174).
+template <class T>
+struct Relax {
+  T omega_s;  // 1 / (tau_s + 1/2)
+  T omega_b;  // 1 / (tau_b + 1/2)
+  T force_s;  // 2 omega_s tau_s
+  T force_b;  // 2 omega_b tau_b
+};
+
+template <class T>
+inline Relax<T> make_relax(double tau_s, double tau_b) {
+  const double ws = 1.0 / (tau_s + 0.5), wb = 1.0 / (tau_b + 0.5);
+  return Relax<T>{(T)ws, (T)wb, (T)(2. * ws * tau_s), (T)(2. * wb * tau_b)};
+}
+
+// Density-deviation, momentum and stress moments of 15 (deviation) values.
+template <class T>
+struct Moments {
+  T R, jx, jy, jz, Sxx, Syy, Szz, Sxy, Sxz, Syz;
+};
+
+template <class T>
+__device__ __forceinline__ Moments<T> moments(const T d[15]) {
+  const T a = d[1] + d[2], ap = d[1] - d[2];
+  const T b = d[3] + d[4], bp = d[3] - d[4];
+  const T c = d[5] + d[6], cp = d[5] - d[6];
+  const T P1 = d[7] + d[8], M1 = d[7] - d[8];
+  const T P2 = d[9] + d[10], M2 = d[9] - d[10];
+  const T P3 = d[11] + d[12], M3 = d[11] - d[12];
+  const T P4 = d[13] + d[14], M4 = d[13] - d[14];
+  const T PPp = P1 + P2, PMp = P1 - P2, MPp = M1 + M2, MMp = M1 - M2;
+  const T PPm = P3 + P4, PMm = P3 - P4, MPm = M3 + M4, MMm = M3 - M4;
+  const T sum = PPp + PPm;
+  Moments<T> m;
+  m.R = d[0] + a + b + c + sum;
+  m.jx = ap + (PPp - PPm);
+  m.jy = bp + (PMp + PMm);
+  m.jz = cp + (MPp + MPm);
+  const T r3 = m.R * (T(1) / T(3));
+  m.Sxx = (a + sum) - r3;
+  m.Syy = (b + sum) - r3;
+  m.Szz = (c + sum) - r3;
+  m.Sxy = PMp - PMm;
+  m.Sxz = MPp - MPm;
+  m.Syz = MMp + MMm;
+  return m;
+}
+
+// Only rho-deviation and momentum (the CalcHydro moments, lb.cu:279-293).
+template <class T>
+__device__ __forceinline__ void hydro_moments(const T d[15], T& R, T& jx, T& jy, T& jz) {
+  const T c1 = d[7] + d[8], c2 = d[9] + d[10], c3 = d[11] + d[12], c4 = d[13] + d[14];
+  const T xp = c1 + c2, xm = c3 + c4;
+  R = d[0] + (d[1] + d[2]) + (d[3] + d[4]) + (d[5] + d[6]) + (xp + xm);
+  jx = (d[1] - d[2]) + (xp - xm);
+  jy = (d[3] - d[4]) + ((c1 - c2) + (c3 - c4));
+  const T z1 = d[7] - d[8], z2 = d[9] - d[10], z3 = d[11] - d[12], z4 = d[13] - d[14];
+  jz = (d[5] - d[6]) + ((z1 + z2) + (z3 + z4));
+}
+
+// out_p = w_p (R + 3 c_p.j + 9/2 Q_p:S): the projection mmi * mode with the
+// ghost modes zero (lb.cu:198-203, 363-369).
+template <class T>
+__device__ __forceinline__ void project(T R, T jx, T jy, T jz, T Sxx, T Syy, T Szz, T Sxy,
+                                        T Sxz, T Syz, T out[15]) {
+  const T w0 = T(2) / T(9), w1 = T(1) / T(9), w7 = T(1) / T(72);
+  const T Tr = Sxx + Syy + Szz;
+  const T Tr3 = Tr * (T(1) / T(3));
+  out[0] = w0 * (R - T(1.5) * Tr);
+  const T ex = R + T(4.5) * (Sxx - Tr3);
+  const T ey = R + T(4.5) * (Syy - Tr3);
+  const T ez = R + T(4.5) * (Szz - Tr3);
+  const T jx3 = T(3) * jx, jy3 = T(3) * jy, jz3 = T(3) * jz;
+  out[1] = w1 * (ex + jx3);
+  out[2] = w1 * (ex - jx3);
+  out[3] = w1 * (ey + jy3);
+  out[4] = w1 * (ey - jy3);
+  out[5] = w1 * (ez + jz3);
+  out[6] = w1 * (ez - jz3);
+  const T A = R + T(3) * Tr;
+  const T Cxy = T(9) * Sxy, Cxz = T(9) * Sxz, Cyz = T(9) * Syz;
+  {  // corners with c_x = +1
+    const T G = A + jx3, Hy = jy3 + Cxy, Hz = jz3 + Cxz;
+    const T K1 = G + Hy, K2 = G - Hy, L1 = Hz + Cyz, L2 = Hz - Cyz;
+    out[7] = w7 * (K1 + L1);
+    out[8] = w7 * (K1 - L1);
+    out[9] = w7 * (K2 + L2);
+    out[10] = w7 * (K2 - L2);
+  }
+  {  // corners with c_x = -1
+    const T G = A - jx3, Hy = jy3 - Cxy, Hz = jz3 - Cxz;
+    const T K1 = G + Hy, K2 = G - Hy, L1 = Hz + Cyz, L2 = Hz - Cyz;
+    out[11] = w7 * (K1 + L1);
+    out[12] = w7 * (K1 - L1);
+    out[13] = w7 * (K2 + L2);
+    out[14] = w7 * (K2 - L2);
+  }
+}
+
+// MRT collision with forcing, lb.cu:121-195, on deviations d_p = f_p - w_p rho0
+// (rho0 = 0 gives the reference's plain distributions).  out may alias d.
+template <class T>
+__device__ __forceinline__ void collide(const T d[15], T Fx, T Fy, T Fz, T rho0,
+                                        const Relax<T>& k, T out[15]) {
+  const Moments<T> m = moments(d);
+  const T rho = rho0 + m.R;
+  const T inv = T(1) / rho;
+  const T ux = (m.jx + T(0.5) * Fx) * inv;
+  const T uy = (m.jy + T(0.5) * Fy) * inv;
+  const T uz = (m.jz + T(0.5) * Fz) * inv;
+  const T usq = ux * ux + uy * uy + uz * uz;
+  const T uF = ux * Fx + uy * Fy + uz * Fz;
+  const T third = T(1) / T(3);
+  const T TrS = m.Sxx + m.Syy + m.Szz;
+  const T tx = m.Sxx - TrS * third, ty = m.Syy - TrS * third, tz = m.Szz - TrS * third;
+  // trace relaxed with omega_b toward rho u.u, plus forcing (lb.cu:163-165)
+  const T TrN = TrS - k.omega_b * (TrS - rho * usq) + k.force_b * uF;
+  const T tr3 = TrN * third;
+  const T ws = k.omega_s, fs = k.force_s;
+  // traceless part relaxed with omega_s, plus forcing (lb.cu:168-178)
+  const T Sxx = tx - ws * (tx - rho * (ux * ux - usq)) + fs * (T(2) * ux * Fx - T(2) * uF) + tr3;
+  const T Syy = ty - ws * (ty - rho * (uy * uy - usq)) + fs * (T(2) * uy * Fy - T(2) * uF) + tr3;
+  const T Szz = tz - ws * (tz - rho * (uz * uz - usq)) + fs * (T(2) * uz * Fz - T(2) * uF) + tr3;
+  const T Sxy = m.Sxy - ws * (m.Sxy - rho * ux * uy) + fs * (ux * Fy + Fx * uy);
+  const T Sxz = m.Sxz - ws * (m.Sxz - rho * ux * uz) + fs * (ux * Fz + Fx * uz);
+  const T Syz = m.Syz - ws * (m.Syz - rho * uy * uz) + fs * (uy * Fz + Fy * uz);
+  project(m.R, m.jx + Fx, m.jy + Fy, m.jz + Fz, Sxx, Syy, Szz, Sxy, Sxz, Syz, out);
+}
+
+// ---- storage formats of the distributions -----------------------------------
+// FP64 and FP32 hold f_p - w_p rho0 (rho0 = 0 for FP64: the plain distribution).
+// BF16 and FP16 hold (f_p - w_p rho0) / w_p so all 15 values share one scale.
+template <class S>
+struct Store;
+template <>
+struct Store<double> {
+  static constexpr bool scaled = false;
+  __device__ static double ld(const double* p) { return *p; }
+  __device__ static void st(double* p, double v) { *p = v; }
+};
+template <>
+struct Store<float> {
+  static constexpr bool scaled = false;
+  __device__ static float ld(const float* p) { return *p; }
+  __device__ static void st(float* p, float v) { *p = v; }
+};
+template <>
+struct Store<__nv_bfloat16> {
+  static constexpr bool scaled = true;
+  __device__ static float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+  __device__ static void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+};
+template <>
+struct Store<__half> {
+  static constexpr bool scaled = true;
+  __device__ static float ld(const __half* p) { return __half2float(*p); }
+  __device__ static void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+
+template <class S, class T>
+__device__ __forceinline__ T dev_from_stored(T g, int p) {
+  return Store<S>::scaled ? g * T(w_of(p)) : g;
+}
+template <class S, class T>
+__device__ __forceinline__ T stored_from_dev(T d, int p) {
+  return Store<S>::scaled ? d * T(1.0 / w_of(p)) : d;
+}
+
+// ---- Peskin 4-point regularised delta (delta.cu:6-25) ------------------------
+template <class T>
+__device__ __forceinline__ T peskin_delta(T x) {
+  const T ax = fabs(x);
+  T root = T(-4) * x * x;
+  T phi = T(-2) * ax;
+  if (ax >= T(2)) return T(0);
+  if (ax >= T(1)) {
+    root += T(12) * ax - T(7);
+    phi += T(5);
+    phi -= sqrt(root);
+  } else {
+    root += T(4) * ax + T(1);
+    phi += T(3);
+    phi += sqrt(root);
+  }
+  return T(0.125) * phi;
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------------
+__device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+  }
+}
+
+// Random stream of one swimmer at one move step.  Block 0 gives the tumble
+// uniform in (0, 1]; blocks 1 and 2 give three Box-Muller normals.
+__device__ __forceinline__ void rng_block(uint64_t seed, uint32_t swimmer, uint64_t step,
+                                          uint32_t block, uint32_t out[4]) {
+  out[0] = swimmer;
+  out[1] = (uint32_t)step;
+  out[2] = (uint32_t)(step >> 32);
+  out[3] = block;
+  philox4x32(out, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+__device__ __forceinline__ float rng_uniform(uint64_t seed, uint32_t swimmer, uint64_t step) {
+  uint32_t x[4];
+  rng_block(seed, swimmer, step, 0u, x);
+  return (float)((x[0] >> 8) + 1u) * 0x1.0p-24f;
+}
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+  const uint64_t m = ((uint64_t)a << 21) | (uint64_t)(b >> 11);
+  return (double)(m + 1u) * 0x1.0p-53;
+}
+__device__ __forceinline__ void rng_normal3(uint64_t seed, uint32_t swimmer, uint64_t step,
+                                            double g[3]) {
+  uint32_t a[4], b[4];
+  rng_block(seed, swimmer, step, 1u, a);
+  rng_block(seed, swimmer, step, 2u, b);
+  const double twopi = 6.283185307179586;
+  const double r1 = sqrt(-2.0 * log(u53(a[0], a[1])));
+  const double r2 = sqrt(-2.0 * log(u53(b[0], b[1])));
+  const double t1 = twopi * u53(a[2], a[3]);
+  const double t2 = twopi * u53(b[2], b[3]);
+  g[0] = r1 * cos(t1);
+  g[1] = r1 * sin(t1);
+  g[2] = r2 * cos(t2);
+}
+
+__device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+}  // namespace lbswim

@@ -1,0 +1,136 @@
+"""ctypes binding of liblbswim's C ABI (include/lbswim_c.h).
+
+The shared library is built in-tree by gpu-swimmers_gb300/build.py.  There is
+no fallback: if the library is missing or cannot be loaded, importing lbswim
+raises ImportError.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_liblbswim.so")
+
+F64, F32, BF16, F16 = 0, 1, 2, 3
+PRECISIONS = {"f64": F64, "float64": F64, "double": F64, "f32": F32, "float32": F32,
+              "float": F32, "bf16": BF16, "bfloat16": BF16, "f16": F16, "float16": F16,
+              "half": F16}
+PRECISION_NAMES = {F64: "f64", F32: "f32", BF16: "bf16", F16: "f16"}
+
+FIELD_RHO, FIELD_U, FIELD_FORCE, FIELD_FOLD, FIELD_FNEW = range(5)
+FIELD_COMPONENTS = {FIELD_RHO: 1, FIELD_U: 3, FIELD_FORCE: 3, FIELD_FOLD: 15, FIELD_FNEW: 15}
+SW_R, SW_V, SW_N = 0, 1, 2
+TR_R, TR_S, TR_V = 0, 1, 2
+COMPAT_INIT_SXZ, COMPAT_SYNC_STEP = 1, 2
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",
+          -5: "not supported"}
+
+
+class LbswimError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, message))
+        self.code = code
+
+
+class LBParamsStruct(C.Structure):
+    _fields_ = [("cs2", C.c_double), ("w", C.c_double * 15), ("xi", (C.c_double * 3) * 15),
+                ("ci", (C.c_int * 3) * 15), ("Q", ((C.c_double * 3) * 3) * 15),
+                ("complement", C.c_int * 15), ("norms", C.c_double * 15),
+                ("mm", (C.c_double * 15) * 15), ("mmi", (C.c_double * 15) * 15),
+                ("tau_s", C.c_double), ("tau_b", C.c_double)]
+
+
+class AddressingStruct(C.Structure):
+    _fields_ = [("size", C.c_int * 3), ("strides", C.c_int * 3), ("n", C.c_int)]
+
+
+class CommonParamsStruct(C.Structure):
+    _fields_ = [("P", C.c_double), ("l", C.c_double), ("alpha", C.c_double),
+                ("mobility", C.c_double), ("translational_advection_off", C.c_int),
+                ("rotational_advection_off", C.c_int), ("seed", C.c_ulonglong)]
+
+
+_VP = C.c_void_p
+_D = C.POINTER(C.c_double)
+
+_PROTOS = {
+    "lbswim_last_error": (C.c_char_p, []),
+    "lbswim_version": (C.c_char_p, []),
+    "lbswim_kernel_launches": (C.c_int, [C.POINTER(C.c_ulonglong)]),
+    "lbswim_lattice_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_int, C.POINTER(_VP)]),
+    "lbswim_lattice_destroy": (C.c_int, [_VP]),
+    "lbswim_lattice_step": (C.c_int, [_VP]),
+    "lbswim_lattice_calc_hydro": (C.c_int, [_VP]),
+    "lbswim_lattice_init_from_hydro": (C.c_int, [_VP]),
+    "lbswim_lattice_zero_force": (C.c_int, [_VP]),
+    "lbswim_lattice_h2d": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_lattice_d2h": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_lattice_get_params": (C.c_int, [_VP, C.POINTER(LBParamsStruct)]),
+    "lbswim_lattice_get_addressing": (C.c_int, [_VP, C.POINTER(AddressingStruct)]),
+    "lbswim_lattice_get_time_step": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "lbswim_lattice_set_time_step": (C.c_int, [_VP, C.c_int]),
+    "lbswim_lattice_get_precision": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "lbswim_lattice_set_compat": (C.c_int, [_VP, C.c_int]),
+    "lbswim_lattice_set_stream": (C.c_int, [_VP, _VP]),
+    "lbswim_lattice_synchronize": (C.c_int, [_VP]),
+    "lbswim_lattice_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP), C.POINTER(C.c_int)]),
+    "lbswim_swimmers_create": (C.c_int, [C.c_int, C.POINTER(CommonParamsStruct), C.POINTER(_VP)]),
+    "lbswim_swimmers_destroy": (C.c_int, [_VP]),
+    "lbswim_swimmers_set_common": (C.c_int, [_VP, C.POINTER(CommonParamsStruct)]),
+    "lbswim_swimmers_get_common": (C.c_int, [_VP, C.POINTER(CommonParamsStruct)]),
+    "lbswim_swimmers_get_num": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "lbswim_swimmers_add_forces": (C.c_int, [_VP, _VP]),
+    "lbswim_swimmers_move": (C.c_int, [_VP, _VP]),
+    "lbswim_swimmers_h2d": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_swimmers_d2h": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_swimmers_get_rng": (C.c_int, [_VP, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
+    "lbswim_swimmers_set_rng": (C.c_int, [_VP, C.c_ulonglong, C.c_ulonglong]),
+    "lbswim_tracers_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "lbswim_tracers_destroy": (C.c_int, [_VP]),
+    "lbswim_tracers_get_num": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "lbswim_tracers_move": (C.c_int, [_VP, _VP]),
+    "lbswim_tracers_h2d": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_tracers_d2h": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_system_step": (C.c_int, [_VP, C.POINTER(_VP), C.c_int, C.POINTER(_VP), C.c_int,
+                                     C.c_int]),
+}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("liblbswim is not built (%s missing); run "
+                          "`python gpu-swimmers_gb300/build.py`" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def check(status):
+    if status != 0:
+        msg = lib.lbswim_last_error()
+        raise LbswimError(status, msg.decode() if msg else "")
+    return status
+
+
+def dptr(a):
+    """Pointer to the data of a C-contiguous float64 numpy array."""
+    if a.dtype.char != "d" or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(_D)
+
+
+def kernel_launches():
+    out = C.c_ulonglong()
+    check(lib.lbswim_kernel_launches(C.byref(out)))
+    return out.value
+
+
+def version():
+    return lib.lbswim_version().decode()

@@ -1,0 +1,194 @@
+/*
+ * lbswim_c.h -- C ABI of liblbswim for GB300 (sm_103a).
+ *
+ * The coupled time step of gpu-swimmers: a D3Q15 MRT lattice-Boltzmann fluid
+ * with periodic boundaries, run-and-tumble swimmers and passive tracers,
+ * coupled through the Peskin 4-point delta.  Every entry point takes plain
+ * pointers and sizes and returns 0 on success or a negative LBSWIM_E* code;
+ * lbswim_last_error() gives the message of the calling thread's last failure.
+ * (The reference prints and calls exit() on any CUDA error, cucall.h:5-14;
+ * here the caller decides.)
+ *
+ * Each entry point names the reference interface it replaces
+ * (rupertnash/gpu-swimmers, paths within that project).
+ *
+ * Layout: every field is element-slowest SoA, as in the reference
+ * (README.md:39).  The site index is i*ny*nz + j*nz + k (lb.cu:55-57).
+ *   rho   [N]        u, force  [3][N]        fOld, fNew  [15][N]
+ *   swimmer r, v, n  [3][n]                  tracer r, s, v  [3][n]
+ * Host buffers passed to the *_h2d / *_d2h calls are FP64 whatever the
+ * lattice's device precision.
+ *
+ * Streams: every launch of a lattice and of the particle arrays used with it
+ * goes to the lattice's stream (default: the legacy default stream, as in the
+ * reference).  Calls return once work is enqueued, except *_d2h, which
+ * synchronise the stream, and lbswim_lattice_step, which synchronises like
+ * Lattice::Step (lb.cu:239) only when LBSWIM_COMPAT_SYNC_STEP is set.
+ */
+#ifndef LBSWIM_C_H
+#define LBSWIM_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define LBSWIM_OK 0
+#define LBSWIM_EINVAL (-1)   /* bad argument */
+#define LBSWIM_ECUDA (-2)    /* CUDA runtime error */
+#define LBSWIM_ENOMEM (-3)   /* device or host allocation failed */
+#define LBSWIM_ESTATE (-4)   /* call not valid in the object's current state */
+#define LBSWIM_ENOTSUP (-5)  /* feature not available for this precision */
+
+/* ---- device precision of the lattice distributions ----------------------- */
+#define LBSWIM_F64 0  /* FP64 storage and arithmetic: the reference's method */
+#define LBSWIM_F32 1  /* FP32 deviations from w_i*rho0, FP32 collision       */
+#define LBSWIM_BF16 2 /* BF16 scaled deviations, FP32 collision              */
+#define LBSWIM_F16 3  /* FP16 scaled deviations, FP32 collision              */
+
+/* ---- lattice fields (Lattice.h:38-50, LatticeData) ----------------------- */
+#define LBSWIM_FIELD_RHO 0
+#define LBSWIM_FIELD_U 1
+#define LBSWIM_FIELD_FORCE 2
+#define LBSWIM_FIELD_FOLD 3
+#define LBSWIM_FIELD_FNEW 4
+
+/* ---- particle fields ------------------------------------------------------ */
+#define LBSWIM_SW_R 0 /* SwimmerArray.h:25-27 */
+#define LBSWIM_SW_V 1
+#define LBSWIM_SW_N 2
+#define LBSWIM_TR_R 0 /* TracerArray.h:13-15 */
+#define LBSWIM_TR_S 1
+#define LBSWIM_TR_V 2
+
+/* ---- compat flags (lbswim_lattice_set_compat) ----------------------------- */
+/* Reproduce lb.cu:356: InitFromHydro builds the xz stress from u_x*u_y.
+ * On by default so results match the reference; inert when u = 0. */
+#define LBSWIM_COMPAT_INIT_SXZ 1
+/* Synchronise the device at the end of every Step, as lb.cu:239 does. */
+#define LBSWIM_COMPAT_SYNC_STEP 2
+
+typedef struct lbswim_lattice lbswim_lattice;
+typedef struct lbswim_swimmers lbswim_swimmers;
+typedef struct lbswim_tracers lbswim_tracers;
+
+/* Same field order and types as the reference's LBParams (LBParams.h:4-30). */
+typedef struct lbswim_lbparams {
+  double cs2;
+  double w[15];
+  double xi[15][3];
+  int ci[15][3];
+  double Q[15][3][3];
+  int complement[15];
+  double norms[15];
+  double mm[15][15];
+  double mmi[15][15];
+  double tau_s;
+  double tau_b;
+} lbswim_lbparams;
+
+/* Same fields as LatticeAddressing (Lattice.h:8-12). */
+typedef struct lbswim_addressing {
+  int size[3];
+  int strides[3];
+  int n;
+} lbswim_addressing;
+
+/* Same fields as CommonParams (SwimmerArray.h:8-16); the bools are widened to
+ * int so the struct has one layout in C, C++ and ctypes. */
+typedef struct lbswim_common_params {
+  double P;
+  double l;
+  double alpha;
+  double mobility;
+  int translational_advection_off;
+  int rotational_advection_off;
+  unsigned long long seed;
+} lbswim_common_params;
+
+/* ---- library -------------------------------------------------------------- */
+const char* lbswim_last_error(void);
+const char* lbswim_version(void);
+/* Number of this library's kernels launched so far in this process. */
+int lbswim_kernel_launches(unsigned long long* count);
+
+/* ---- Lattice (lb.cu, Lattice.h) ------------------------------------------- */
+/* Lattice::Lattice(nx, ny, nz, tau_s, tau_b), lb.cu:40-63.  precision selects
+ * the device storage (LBSWIM_F64 reproduces the reference). */
+int lbswim_lattice_create(int nx, int ny, int nz, double tau_s, double tau_b, int precision,
+                          lbswim_lattice** out);
+/* Lattice::~Lattice, lb.cu:66-67. */
+int lbswim_lattice_destroy(lbswim_lattice* lat);
+/* Lattice::Step, lb.cu:220-247: collide, stream, swap fOld/fNew, time_step++. */
+int lbswim_lattice_step(lbswim_lattice* lat);
+/* Lattice::CalcHydro, lb.cu:297-312: rho, u from fOld and force. */
+int lbswim_lattice_calc_hydro(lbswim_lattice* lat);
+/* Lattice::InitFromHydro, lb.cu:373-388: fOld from rho, u. */
+int lbswim_lattice_init_from_hydro(lbswim_lattice* lat);
+/* Lattice::ZeroForce, lb.cu:413-428. */
+int lbswim_lattice_zero_force(lbswim_lattice* lat);
+/* SharedArray<double>::H2D / D2H (Shared.cu:15-27) of one LatticeData member;
+ * `host` holds count = (1, 3, 3, 15, 15)[field] * N doubles. */
+int lbswim_lattice_h2d(lbswim_lattice* lat, int field, const double* host);
+int lbswim_lattice_d2h(lbswim_lattice* lat, int field, double* host);
+/* Lattice::params.host, Lattice::addr.host, Lattice::time_step (Lattice.h:54-58). */
+int lbswim_lattice_get_params(const lbswim_lattice* lat, lbswim_lbparams* out);
+int lbswim_lattice_get_addressing(const lbswim_lattice* lat, lbswim_addressing* out);
+int lbswim_lattice_get_time_step(const lbswim_lattice* lat, int* out);
+int lbswim_lattice_set_time_step(lbswim_lattice* lat, int time_step); /* lb.pyx:237-244 */
+int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out);
+/* No reference counterpart: behaviour switches and stream binding. */
+int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags);
+int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
+int lbswim_lattice_synchronize(lbswim_lattice* lat);
+/* Device address and element size (8, 4 or 2) of a field's current buffer. */
+int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, int* elem_bytes);
+
+/* ---- SwimmerArray (SwimmerArray.cu, SwimmerArray.h) ------------------------ */
+/* SwimmerArray::SwimmerArray(n, p), SwimmerArray.cu:16-25.  The random stream
+ * is keyed by (p->seed, swimmer index, move step), fixed at construction like
+ * the reference's curand_init. */
+int lbswim_swimmers_create(int n, const lbswim_common_params* p, lbswim_swimmers** out);
+int lbswim_swimmers_destroy(lbswim_swimmers* sw);
+/* SharedItem<CommonParams>::H2D after a property set (swimmers.pyx:21-68). */
+int lbswim_swimmers_set_common(lbswim_swimmers* sw, const lbswim_common_params* p);
+int lbswim_swimmers_get_common(const lbswim_swimmers* sw, lbswim_common_params* out);
+int lbswim_swimmers_get_num(const lbswim_swimmers* sw, int* out);
+/* SwimmerArray::AddForces, SwimmerArray.cu:114-121 (deterministic order). */
+int lbswim_swimmers_add_forces(lbswim_swimmers* sw, lbswim_lattice* lat);
+/* SwimmerArray::Move, SwimmerArray.cu:212-220. */
+int lbswim_swimmers_move(lbswim_swimmers* sw, lbswim_lattice* lat);
+/* SharedArray<double>::H2D / D2H of r, v or n (3*n doubles). */
+int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host);
+int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host);
+/* The random-stream state that SharedArray<RandState> prng holds in the
+ * reference (SwimmerArray.h:28): the key seed and the next move step. */
+int lbswim_swimmers_get_rng(const lbswim_swimmers* sw, unsigned long long* seed,
+                            unsigned long long* step);
+int lbswim_swimmers_set_rng(lbswim_swimmers* sw, unsigned long long seed,
+                            unsigned long long step);
+
+/* ---- TracerArray (TracerArray.cu, TracerArray.h) --------------------------- */
+/* TracerArray::TracerArray(n), TracerArray.cu:5-10. */
+int lbswim_tracers_create(int n, lbswim_tracers** out);
+int lbswim_tracers_destroy(lbswim_tracers* tr);
+int lbswim_tracers_get_num(const lbswim_tracers* tr, int* out);
+/* TracerArray::Move, TracerArray.cu:45-52. */
+int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat);
+int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host);
+int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
+
+/* ---- coupled step (System.Step, System.py:9-16) ---------------------------- */
+/* nsteps repetitions of: ZeroForce; AddForces for every swimmer array; Step;
+ * CalcHydro; Move for every swimmer array, then every tracer array.  Results
+ * are those of the same sequence of single calls. */
+int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, int n_swimmers,
+                       lbswim_tracers* const* tracers, int n_tracers, int nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,140 @@
+"""Python surface behaviour on the GPU: README scenario, fields, pickle, errors."""
+import pickle
+
+import numpy as np
+import pytest
+
+import oracle as O
+from gpu_harness import build_gpu, snapshot
+from helpers import TOL_F64, rel_l2, rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+def test_readme_example_runs_unchanged():
+    from lbswim import lb, swimmers, tracers
+    from lbswim.System import System
+    tau = 0.25
+    eta = tau / 3
+    lat = lb.Lattice(16, 16, 16, tau, tau)
+    lat.rho[:] = 1.0
+    lat.rho.H2D()
+    lat.u[:] = 0.0
+    lat.u.H2D()
+    lat.ZeroForce()
+    system = System(lat)
+    cp = swimmers.CommonParams()
+    cp.P = 1e-3
+    cp.l = 0.1
+    cp.alpha = 0.01
+    a = 0.1
+    hydroRadius = 1.5
+    cp.mobility = (1.0 / a - 1.0 / hydroRadius) / (6.0 * np.pi * eta)
+    cp.translational_advection_off = False
+    cp.rotational_advection_off = False
+    cp.seed = 1234
+    sw = swimmers.Array(1, cp)
+    sw.r[:] = 8
+    sw.n[:] = [[0], [0], [1]]
+    sw.v[:] = 0.
+    sw.H2D()
+    system.AddThing(sw)
+    tr = tracers.Array(16 ** 3)
+    tr.r[:] = np.mgrid[:16, :16, :16].reshape(3, 16 ** 3)
+    tr.v[:] = 0.
+    tr.H2D()
+    system.AddThing(tr)
+    lat.InitFromHydro()
+    traj = []
+    while lat.time_step < 100:
+        if lat.time_step % 10 == 0:
+            sw.D2H()
+            traj.append(sw.r[:, 0].copy())
+        system.Step()
+    assert lat.time_step == 100
+    traj = np.array(traj)
+    assert np.all(np.diff(traj[:, 2]) > 0)  # swims along +z
+    assert lat.params.eta == pytest.approx(tau / 3)
+    assert lat.addr.size == (16, 16, 16) and lat.addr.n == 4096
+    assert lat.rho.shape == (1, 16, 16, 16) and lat.fOld.shape == (15, 16, 16, 16)
+
+
+def test_params_tables_match_oracle():
+    from lbswim import lb
+    lat = lb.Lattice(4, 4, 4, 0.7, 0.9)
+    P = lat.params
+    ref = O.params_dict(O.params(0.7, 0.9))
+    for k in ("w", "xi", "ci", "Q", "complement", "norms", "mm", "mmi"):
+        assert np.array_equal(getattr(P, k), ref[k]), k
+    assert P.cs2 == ref["cs2"] and P.tau_s == 0.7 and P.tau_b == 0.9
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 0.0), ("f32", 1e-9), ("bf16", 2e-5),
+                                           ("f16", 1e-6)])
+def test_field_roundtrip(precision, tol):
+    from lbswim import lb
+    lat = lb.Lattice(10, 12, 14, 0.8, 0.8, precision=precision)
+    rng = np.random.default_rng(0)
+    w = lat.params.w.reshape(15, 1, 1, 1)
+    f = w * (1.0 + 1e-3 * rng.standard_normal((15, 10, 12, 14)))
+    lat.fOld[:] = f
+    lat.fOld.H2D()
+    lat.fOld[:] = 0
+    lat.fOld.D2H()
+    assert np.max(np.abs(lat.fOld.data - f)) <= tol
+    for name in ("rho", "u", "force"):
+        fld = getattr(lat, name)
+        vals = rng.standard_normal(fld.shape)
+        fld[:] = vals
+        fld.H2D()
+        fld[:] = 0
+        fld.D2H()
+        assert np.max(np.abs(fld.data - vals)) <= (0 if precision == "f64" else 1e-6)
+
+
+def test_zero_force_then_read_is_zero():
+    from lbswim import lb
+    lat = lb.Lattice(8, 8, 8, 0.8, 0.8)
+    lat.force[:] = 1.0
+    lat.force.H2D()
+    lat.ZeroForce()
+    lat.force.D2H()
+    assert np.all(lat.force.data == 0)
+
+
+def test_pickle_resume_is_exact():
+    case = O.random_case((12, 14, 16), 40, 100, seed=31, alpha=0.3)
+    lat, sw, tr, system = build_gpu(case)
+    system.Step(10)
+    blob = pickle.dumps((lat, sw, tr))
+    system.Step(15)
+    end = snapshot(lat, sw, tr)
+    lat2, sw2, tr2 = pickle.loads(blob)
+    from lbswim.System import System
+    s2 = System(lat2)
+    s2.AddThing(sw2)
+    s2.AddThing(tr2)
+    # the reference pickles only fOld; rho/u are recomputed by the first step
+    assert lat2.time_step == 10
+    s2.Step(15)
+    res = snapshot(lat2, sw2, tr2)
+    for k in ("f", "rho", "u", "sw_r", "sw_n", "tr_r"):
+        assert np.array_equal(res[k], end[k]), k
+
+
+def test_invalid_field_raises():
+    from lbswim import _lib, lb
+    lat = lb.Lattice(4, 4, 4, 0.8, 0.8)
+    buf = np.zeros(4 * 4 * 4)
+    with pytest.raises(_lib.LbswimError):
+        _lib.check(_lib.lib.lbswim_lattice_h2d(lat._h, 7, _lib.dptr(buf)))
+
+
+def test_kernel_launch_counter_advances():
+    from lbswim import _lib
+    before = _lib.kernel_launches()
+    case = O.random_case((8, 8, 8), 4, 10, seed=1)
+    lat, sw, tr, system = build_gpu(case)
+    system.Step(3)
+    lat.synchronize()
+    assert _lib.kernel_launches() - before >= 3 * 6
