@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Coupled-step benchmark: D3Q15 MRT LB + swimmers + tracers on one GB300.
+
+Default workload: a 256^3 periodic lattice (tau_s = tau_b = 0.8,
+rho = 1 + 1e-3 U[0,1), u = 0) with 65,536 run-and-tumble swimmers and
+1,048,576 tracers at seeded uniform positions, FP32 deviation storage with
+FP32 collision, advanced with the coupled step ZeroForce / AddForces / Step /
+CalcHydro / Move.  A step is one coupled step of the whole lattice.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision f32|bf16|f16|f64] [--size S]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput in
+GLUPS (lattice-site updates per second); `e2e` is the same metric through the
+public Python API with host buffers, the per-step swimmer read-back and the
+initial upload inside the timed region.  `--impl reference` times the
+reference's method (the FP64 CPU restatement in oracle/, all host threads) on
+a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gpu-swimmers_gb300"))
+
+METRIC = "coupled-step GLUPS & % HBM roofline; p50/p99 latency, batched vs plain FP64"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload(size, nsw, ntr, seed=42, tau=0.8, P=1e-3, l=0.5, alpha=0.01):
+    """Seeded synthetic inputs: rho = 1 + 1e-3 U[0,1), u = 0, particles uniform in
+    the box, swimmer orientations uniform on the sphere."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = size
+    N = nx * ny * nz
+    L = np.array(size, dtype=np.float64).reshape(3, 1)
+    rho = 1.0 + 1e-3 * rng.random(N)
+    nv = rng.standard_normal((3, nsw))
+    if nsw:
+        nv /= np.linalg.norm(nv, axis=0, keepdims=True)
+    eta = tau / 3.0
+    sw = {"n": nsw, "P": P, "l": l, "alpha": alpha,
+          "mobility": (1.0 / 0.1 - 1.0 / 1.5) / (6.0 * np.pi * eta),
+          "translational_advection_off": False, "rotational_advection_off": False,
+          "seed": seed * 7919 + 17, "r": rng.random((3, nsw)) * L, "nvec": nv,
+          "v": np.zeros((3, nsw))}
+    tr = {"n": ntr, "r": rng.random((3, ntr)) * L, "v": np.zeros((3, ntr))}
+    return {"size": tuple(size), "tau_s": tau, "tau_b": tau, "rho": rho, "u": 0.0,
+            "swimmers": sw, "tracers": tr}
+
+
+def scaled_counts(side, base_side=256, nsw=65536, ntr=1048576):
+    f = (side / base_side) ** 3
+    return max(1, int(round(nsw * f))), max(1, int(round(ntr * f)))
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def build_objects(case, precision):
+    from lbswim import lb, swimmers, tracers
+    from lbswim.System import System
+    nx, ny, nz = case["size"]
+    lat = lb.Lattice(nx, ny, nz, case["tau_s"], case["tau_b"], precision=precision)
+    sw_d = case["swimmers"]
+    cp = swimmers.CommonParams()
+    for k in ("P", "l", "alpha", "mobility", "translational_advection_off",
+              "rotational_advection_off", "seed"):
+        setattr(cp, k, sw_d[k])
+    sw = swimmers.Array(sw_d["n"], cp)
+    tr = tracers.Array(case["tracers"]["n"])
+    system = System(lat)
+    system.AddThing(sw)
+    system.AddThing(tr)
+    return lat, sw, tr, system
+
+
+def upload(case, lat, sw, tr):
+    """Host -> device copy of the whole initial state; returns bytes moved."""
+    nx, ny, nz = case["size"]
+    N = nx * ny * nz
+    lat.rho[:] = np.broadcast_to(case["rho"], (N,)).reshape(1, nx, ny, nz)
+    lat.rho.H2D()
+    lat.u[:] = np.broadcast_to(case["u"], (3 * N,)).reshape(3, nx, ny, nz)
+    lat.u.H2D()
+    lat.ZeroForce()
+    s = case["swimmers"]
+    sw.r[:] = s["r"]
+    sw.n[:] = s["nvec"]
+    sw.v[:] = s["v"]
+    sw.H2D()
+    t = case["tracers"]
+    tr.r[:] = t["r"]
+    tr.v[:] = t["v"]
+    tr.s[:] = 0.0
+    tr.H2D()
+    lat.InitFromHydro()
+    return 8 * N * 4 + 8 * 9 * s["n"] + 16 + 8 * 9 * t["n"]
+
+
+def algorithmic_bytes(N, nsw, ntr, s_f, s_h):
+    """Per step: f read + write, force read, rho + u write per site; r, n (or s)
+    read + write and v write per particle."""
+    lb_bytes = N * (30 * s_f + 3 * s_h + 4 * s_h)
+    return lb_bytes, lb_bytes + 120 * nsw + 120 * ntr
+
+
+def run_cpu_port(side, steps_budget_s, min_steps=3, threads=None, case=None):
+    """Time the FP64 CPU restatement of the reference on a side^3 sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = threads or os.cpu_count()
+    O.set_threads(threads)
+    if case is None:
+        nsw, ntr = scaled_counts(side)
+        case = workload((side, side, side), nsw, ntr)
+    s = O.make_system(case)
+    s.step(1)
+    t0 = time.perf_counter()
+    n = 0
+    while n < min_steps or time.perf_counter() - t0 < steps_budget_s:
+        s.step(1)
+        n += 1
+    dt = time.perf_counter() - t0
+    N = side ** 3
+    return {"value": N * n / dt / 1e9, "unit": "GLUPS", "cores": O.get_threads(), "kind": "port",
+            "sample": "%d^3 lattice, %d swimmers, %d tracers (256^3 densities), %d coupled FP64 "
+                      "steps in %.1f s, oracle/lbswim_oracle.c with OpenMP"
+                      % (side, case["swimmers"]["n"], case["tracers"]["n"], n, dt)}
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count()
+    O.set_threads(threads)
+    # calibrate the per-site cost on a 64^3 sample, then size the sample so the
+    # whole warm-up + timed run stays within about two minutes
+    nsw, ntr = scaled_counts(64)
+    cal = O.make_system(workload((64, 64, 64), nsw, ntr))
+    t0 = time.perf_counter()
+    cal.step(2)
+    per_site = (time.perf_counter() - t0) / 2 / 64 ** 3
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    side = int(max(16, min(args.size, (budget / per_site) ** (1.0 / 3.0))))
+    nsw, ntr = scaled_counts(side)
+    case = workload((side, side, side), nsw, ntr)
+    s = O.make_system(case)
+    s.step(args.warmup)
+    t0 = time.perf_counter()
+    s.step(args.steps)
+    dt = time.perf_counter() - t0
+    N = side ** 3
+    value = N * args.steps / dt / 1e9
+    sample = ("%d^3 lattice, %d swimmers, %d tracers (the %d^3 workload's densities), FP64, "
+              "oracle/lbswim_oracle.c (the reference's method restated in C) on %d threads"
+              % (side, nsw, ntr, args.size, threads))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args, world),
+            "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, world):
+    nsw, ntr = scaled_counts(args.size)
+    return {"workload": "coupled step, %d^3 D3Q15 MRT lattice, %d swimmers, %d tracers, %s "
+                        "distributions" % (args.size, nsw, ntr, args.precision),
+            "lattice": [args.size] * 3, "swimmers": nsw, "tracers": ntr, "tau": 0.8,
+            "precision": args.precision, "parallelism": "replicas x%d" % world,
+            "l2": "no flush: each step streams %.2f GB of distributions, larger than the "
+                  "129 MB L2" % (2 * 15 * args.size ** 3 * {"f64": 8, "f32": 4}.get(
+                      args.precision, 2) / 1e9)}
+
+
+def load_traffic(precision, side):
+    path = os.path.join(ROOT, "profiles", "fused_step_%s_traffic.json" % precision)
+    try:
+        with open(path) as fh:
+            rec = json.load(fh)
+        # bytes per launch scale with the sites of the lattice
+        return rec["dram_bytes_per_site"] * side ** 3
+    except Exception:
+        return None
+
+
+def our_arm(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from lbswim import _lib
+    side = args.size
+    nsw, ntr = scaled_counts(side)
+    case = workload((side, side, side), nsw, ntr, seed=42 + rank)
+    N = side ** 3
+    lat, sw, tr, system = build_objects(case, args.precision)
+    upload(case, lat, sw, tr)
+    stream = torch.cuda.default_stream()  # the library launches on the legacy default stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        system.Step()
+    barrier()
+    lat.set_timing(True)
+    lat.read_timing()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = _lib.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        system.Step()
+    ev1.record(stream)
+    barrier()
+    launches = _lib.kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    lb_ms, lb_n = lat.read_timing()
+    lat.set_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = N * args.steps * world / (ms / 1e3) / 1e9
+
+    # end to end through the public API: upload, init, K steps each followed by
+    # the swimmer read-back of the README loop, final read-back of rho and u
+    barrier()
+    t0 = time.perf_counter()
+    h2d = upload(case, lat, sw, tr)
+    d2h = 0
+    for _ in range(args.steps):
+        system.Step()
+        sw.D2H()
+        d2h += 8 * 9 * nsw + 16
+    lat.rho.D2H()
+    lat.u.D2H()
+    d2h += 8 * 4 * N
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": N * args.steps * world / e2e_s / 1e9, "unit": "GLUPS",
+           "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+           "api": "lbswim.System.Step() + swimmers.Array.D2H() per step (Python -> C ABI)"}
+
+    s_f = {"f64": 8, "f32": 4}.get(args.precision, 2)
+    s_h = 8 if args.precision == "f64" else 4
+    lb_bytes, step_bytes = algorithmic_bytes(N, nsw, ntr, s_f, s_h)
+    peak, peak_kind = measured_peak()
+    lb_avg_s = lb_ms / max(lb_n, 1) / 1e3
+    achieved = lb_bytes / lb_avg_s / 1e9
+    traffic = load_traffic(args.precision, side)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "k_fused_step" if args.precision != "f64" else "k_step_push_f64",
+                "kernel_ms": lb_avg_s * 1e3, "bytes_per_launch": lb_bytes,
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+                if peak_kind == "measured" else "fallback 6.8 TB/s"}
+    step_ach = step_bytes / (ms_step / 1e3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "GLUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "f32" else args.precision, "data": "synthetic",
+            "config": config_dict(args, world), "clocks": clk, "e2e": e2e,
+            "gpu_launches": int(launches), "roofline": roofline,
+            "step_roofline": {"achieved": step_ach, "peak": peak, "unit": "GB/s",
+                              "frac": step_ach / peak, "bytes_per_step": step_bytes}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = run_cpu_port(min(96, side), 12.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", default="f32", choices=["f64", "f32", "bf16", "f16"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        our_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

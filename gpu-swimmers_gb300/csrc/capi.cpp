@@ -241,6 +241,21 @@ int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, 
   API_END
 }
 
+int lbswim_lattice_set_timing(lbswim_lattice* lat, int enable) {
+  API_BEGIN
+  check_lattice(lat);
+  LAT(lat)->timing = enable != 0;
+  API_END
+}
+
+int lbswim_lattice_get_timing(lbswim_lattice* lat, double* total_ms, int* launches) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(total_ms && launches, "NULL argument");
+  lattice_read_timing(LAT(lat), total_ms, launches);
+  API_END
+}
+
 // ---- SwimmerArray ----------------------------------------------------------------
 static void check_common(const lbswim_common_params* p) {
   REQUIRE(p, "CommonParams is NULL");
@@ -368,6 +383,24 @@ int lbswim_swimmers_set_rng(lbswim_swimmers* sw, unsigned long long seed, unsign
   REQUIRE(sw, "swimmers handle is NULL");
   SW(sw)->seed = seed;
   SW(sw)->step = step;
+  API_END
+}
+
+int lbswim_lattice_interp_velocity(lbswim_lattice* lat, int npoints, const double* r, double* v) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(npoints >= 0, "npoints must be non-negative");
+  REQUIRE(npoints == 0 || (r && v), "NULL argument");
+  lattice_interp_velocity(LAT(lat), npoints, r, v);
+  API_END
+}
+
+int lbswim_rng_draws(unsigned long long seed, int n, unsigned long long step, float* uniform,
+                     double* normal) {
+  API_BEGIN
+  REQUIRE(n >= 0, "n must be non-negative");
+  REQUIRE(n == 0 || (uniform && normal), "NULL argument");
+  rng_draws(seed, n, step, uniform, normal);
   API_END
 }
 

@@ -399,6 +399,14 @@ void lattice_free(Lattice* L) {
                   L->spread.order, L->spread.ends};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (auto& p : L->timed) {
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+  for (auto& p : L->event_pool) {
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
 }
 
 static double* staging(Lattice* L, size_t elems) {
@@ -482,8 +490,39 @@ static void fused_step_t(Lattice* L) {
     launch_fused<S, 32, 8>(L, a);
 }
 
+static std::pair<cudaEvent_t, cudaEvent_t> timing_pair(Lattice* L) {
+  if (!L->event_pool.empty()) {
+    auto p = L->event_pool.back();
+    L->event_pool.pop_back();
+    return p;
+  }
+  std::pair<cudaEvent_t, cudaEvent_t> p;
+  LB_CUDA(cudaEventCreate(&p.first));
+  LB_CUDA(cudaEventCreate(&p.second));
+  return p;
+}
+
+void lattice_read_timing(Lattice* L, double* total_ms, int* launches) {
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  double sum = 0.0;
+  for (auto& p : L->timed) {
+    float ms = 0.f;
+    LB_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+    sum += ms;
+    L->event_pool.push_back(p);
+  }
+  *total_ms = sum;
+  *launches = (int)L->timed.size();
+  L->timed.clear();
+}
+
 void lattice_step(Lattice* L) {
   const int nx = L->size[0], ny = L->size[1], nz = L->size[2];
+  std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+  if (L->timing) {
+    ev = timing_pair(L);
+    LB_CUDA(cudaEventRecord(ev.first, L->stream));
+  }
   if (L->precision == LBSWIM_F64) {
     dim3 grid((nz + 31) / 32, (ny + 7) / 8, nx);
     k_step_push_f64<<<grid, dim3(32, 8), 0, L->stream>>>(
@@ -496,6 +535,10 @@ void lattice_step(Lattice* L) {
       case LBSWIM_BF16: fused_step_t<__nv_bfloat16>(L); break;
       default: fused_step_t<__half>(L); break;
     }
+  }
+  if (L->timing) {
+    LB_CUDA(cudaEventRecord(ev.second, L->stream));
+    L->timed.push_back(ev);
   }
   L->cur ^= 1;
   L->f_version++;

@@ -5,6 +5,8 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "lbswim_c.h"
 
@@ -77,6 +79,10 @@ struct Lattice {
   double* staging = nullptr;  // FP64 staging for conversions
   size_t staging_elems = 0;
   int fused_tile = 0;  // 0 = 32x8 cross-section, 1 = 16x16
+  // CUDA-event timing of the LB step kernel (lbswim_lattice_set_timing)
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;  // recorded, not yet read
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> event_pool;
 };
 
 struct Swimmers {
@@ -107,10 +113,14 @@ void lattice_calc_hydro(Lattice* L);
 void lattice_h2d(Lattice* L, int field, const double* host);
 void lattice_d2h(Lattice* L, int field, double* host);
 void fill_params(lbswim_lbparams* p, double tau_s, double tau_b);
+void lattice_read_timing(Lattice* L, double* total_ms, int* launches);
 
 // particles.cu
 void swimmers_add_forces(Swimmers* S, Lattice* L);
 void swimmers_move(Swimmers* S, Lattice* L);
 void tracers_move(Tracers* T, Lattice* L);
+void lattice_interp_velocity(Lattice* L, int npoints, const double* r_host, double* v_host);
+void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,
+               double* g_host);
 
 }  // namespace lbswim

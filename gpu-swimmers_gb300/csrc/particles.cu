@@ -350,6 +350,27 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
   }
 }
 
+template <class U, class T>
+__global__ void k_interp_points(int np, const double* __restrict__ r, double* __restrict__ v,
+                                Dims D, const U* __restrict__ u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const double rr[3] = {r[i], r[np + i], r[2 * np + i]};
+  T vv[3];
+  interp_velocity<U, T>(u, D, rr, vv);
+  for (int d = 0; d < 3; ++d) v[np * d + i] = (double)vv[d];
+}
+
+__global__ void k_rng_draws(unsigned long long seed, int n, unsigned long long step,
+                            float* __restrict__ uni, double* __restrict__ g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uni[i] = rng_uniform(seed, (uint32_t)i, step);
+  double nn[3];
+  rng_normal3(seed, (uint32_t)i, step, nn);
+  for (int d = 0; d < 3; ++d) g[n * d + i] = nn[d];
+}
+
 // ---- host side -----------------------------------------------------------------
 static Dims make_dims(const Lattice* L) {
   Dims D;
@@ -460,6 +481,57 @@ void tracers_move(Tracers* T, Lattice* L) {
     k_tracers_move<float, float><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
                                                                (const float*)L->u);
   LB_CHECK_LAUNCH(1);
+}
+
+void lattice_interp_velocity(Lattice* L, int np, const double* r_host, double* v_host) {
+  if (np <= 0) return;
+  const Dims D = make_dims(L);
+  double *r = nullptr, *v = nullptr;
+  LB_CUDA(cudaMalloc(&r, sizeof(double) * 3 * np));
+  cudaError_t e = cudaMalloc(&v, sizeof(double) * 3 * np);
+  if (e != cudaSuccess) {
+    cudaFree(r);
+    LB_CUDA(e);
+  }
+  try {
+    LB_CUDA(cudaMemcpyAsync(r, r_host, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, L->stream));
+    if (L->precision == LBSWIM_F64)
+      k_interp_points<double, double><<<(np + 255) / 256, 256, 0, L->stream>>>(np, r, v, D,
+                                                                              (const double*)L->u);
+    else
+      k_interp_points<float, float><<<(np + 255) / 256, 256, 0, L->stream>>>(np, r, v, D,
+                                                                            (const float*)L->u);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaMemcpyAsync(v_host, v, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, L->stream));
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+  } catch (...) {
+    cudaFree(r);
+    cudaFree(v);
+    throw;
+  }
+  cudaFree(r);
+  cudaFree(v);
+}
+
+void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,
+               double* g_host) {
+  if (n <= 0) return;
+  float* u = nullptr;
+  double* g = nullptr;
+  LB_CUDA(cudaMalloc(&u, sizeof(float) * n));
+  cudaError_t e = cudaMalloc(&g, sizeof(double) * 3 * n);
+  if (e != cudaSuccess) {
+    cudaFree(u);
+    LB_CUDA(e);
+  }
+  k_rng_draws<<<(n + 255) / 256, 256>>>(seed, n, step, u, g);
+  cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) le = cudaMemcpy(u_host, u, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  if (le == cudaSuccess) le = cudaMemcpy(g_host, g, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost);
+  cudaFree(u);
+  cudaFree(g);
+  LB_CUDA(le);
+  count_launches(1);
 }
 
 }  // namespace lbswim

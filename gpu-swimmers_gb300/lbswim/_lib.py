@@ -75,6 +75,8 @@ _PROTOS = {
     "lbswim_lattice_set_stream": (C.c_int, [_VP, _VP]),
     "lbswim_lattice_synchronize": (C.c_int, [_VP]),
     "lbswim_lattice_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP), C.POINTER(C.c_int)]),
+    "lbswim_lattice_set_timing": (C.c_int, [_VP, C.c_int]),
+    "lbswim_lattice_get_timing": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "lbswim_swimmers_create": (C.c_int, [C.c_int, C.POINTER(CommonParamsStruct), C.POINTER(_VP)]),
     "lbswim_swimmers_destroy": (C.c_int, [_VP]),
     "lbswim_swimmers_set_common": (C.c_int, [_VP, C.POINTER(CommonParamsStruct)]),
@@ -86,6 +88,9 @@ _PROTOS = {
     "lbswim_swimmers_d2h": (C.c_int, [_VP, C.c_int, _D]),
     "lbswim_swimmers_get_rng": (C.c_int, [_VP, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "lbswim_swimmers_set_rng": (C.c_int, [_VP, C.c_ulonglong, C.c_ulonglong]),
+    "lbswim_lattice_interp_velocity": (C.c_int, [_VP, C.c_int, _D, _D]),
+    "lbswim_rng_draws": (C.c_int, [C.c_ulonglong, C.c_int, C.c_ulonglong,
+                                   C.POINTER(C.c_float), _D]),
     "lbswim_tracers_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "lbswim_tracers_destroy": (C.c_int, [_VP]),
     "lbswim_tracers_get_num": (C.c_int, [_VP, C.POINTER(C.c_int)]),
@@ -130,6 +135,16 @@ def kernel_launches():
     out = C.c_ulonglong()
     check(lib.lbswim_kernel_launches(C.byref(out)))
     return out.value
+
+
+def rng_draws(seed, n, step):
+    """Device-side draws of the swimmer random stream: (uniform[n], normal[3, n])."""
+    import numpy as np
+    u = np.zeros(n, dtype=np.float32)
+    g = np.zeros((3, n), dtype=np.float64)
+    check(lib.lbswim_rng_draws(int(seed), int(n), int(step),
+                               u.ctypes.data_as(C.POINTER(C.c_float)), dptr(g)))
+    return u, g
 
 
 def version():

@@ -200,6 +200,24 @@ class Lattice:
     def synchronize(self):
         _lib.check(_lib.lib.lbswim_lattice_synchronize(self._h))
 
+    def set_timing(self, enable=True):
+        """Bracket every LB step kernel of this lattice with CUDA events."""
+        _lib.check(_lib.lib.lbswim_lattice_set_timing(self._h, int(bool(enable))))
+
+    def read_timing(self):
+        """(total device ms, launches) of the LB step kernel since the last read."""
+        ms, n = C.c_double(), C.c_int()
+        _lib.check(_lib.lib.lbswim_lattice_get_timing(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def interp_velocity(self, r):
+        """InterpVelocity (interp.cu:8-47) of the current u at points r[3, n]."""
+        r = np.ascontiguousarray(np.asarray(r, dtype=np.float64).reshape(3, -1))
+        v = np.zeros_like(r)
+        _lib.check(_lib.lib.lbswim_lattice_interp_velocity(self._h, r.shape[1], _lib.dptr(r),
+                                                           _lib.dptr(v)))
+        return v
+
     def device_ptr(self, field):
         ptr, elem = C.c_void_p(), C.c_int()
         _lib.check(_lib.lib.lbswim_lattice_device_ptr(self._h, int(field), C.byref(ptr),

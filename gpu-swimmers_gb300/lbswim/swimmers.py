@@ -79,6 +79,9 @@ class Array:
         self._common = CommonParams()
         self._common._adopt(self)
         self.prng = shared.PrngArray(self)
+        # As the reference's constructor does (SwimmerArray.cu:24), pull the
+        # freshly seeded stream state so a later H2D() pushes it back intact.
+        self.prng.D2H()
 
     def _shared(self, which):
         h = self._h
@@ -90,7 +93,7 @@ class Array:
             _lib.check(_lib.lib.lbswim_swimmers_d2h(h, which, _lib.dptr(buf)))
 
         a = shared.Array(self, 3 * self.num, h2d, d2h)
-        a.view.shape = (3, self.num)
+        a.view = a.view.reshape(3, self.num)
         return a
 
     def __del__(self):

@@ -28,7 +28,7 @@ class Array:
             _lib.check(_lib.lib.lbswim_tracers_d2h(h, which, _lib.dptr(buf)))
 
         a = shared.Array(self, 3 * self.num, h2d, d2h)
-        a.view.shape = (3, self.num)
+        a.view = a.view.reshape(3, self.num)
         return a
 
     def __del__(self):

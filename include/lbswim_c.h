@@ -146,6 +146,12 @@ int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
 int lbswim_lattice_synchronize(lbswim_lattice* lat);
 /* Device address and element size (8, 4 or 2) of a field's current buffer. */
 int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, int* elem_bytes);
+/* When enabled, every LB step kernel of this lattice is bracketed by CUDA
+ * events on the lattice's stream.  get_timing synchronises the stream and
+ * returns the summed device time (ms) and number of timed launches since the
+ * previous call. */
+int lbswim_lattice_set_timing(lbswim_lattice* lat, int enable);
+int lbswim_lattice_get_timing(lbswim_lattice* lat, double* total_ms, int* launches);
 
 /* ---- SwimmerArray (SwimmerArray.cu, SwimmerArray.h) ------------------------ */
 /* SwimmerArray::SwimmerArray(n, p), SwimmerArray.cu:16-25.  The random stream
@@ -170,6 +176,17 @@ int lbswim_swimmers_get_rng(const lbswim_swimmers* sw, unsigned long long* seed,
                             unsigned long long* step);
 int lbswim_swimmers_set_rng(lbswim_swimmers* sw, unsigned long long seed,
                             unsigned long long step);
+
+/* InterpVelocity (interp.cu:8-47) at npoints arbitrary points: r and v are
+ * [3][npoints] host arrays.  Reads the lattice's current u. */
+int lbswim_lattice_interp_velocity(lbswim_lattice* lat, int npoints, const double* r, double* v);
+
+/* Draws of the swimmer random stream, computed on the device for swimmers
+ * 0..n-1 at one move step: the tumble uniform in (0, 1] (uniform[n]) and the
+ * three normals of a tumble (normal[3][n]).  Stands in for the cuRAND calls of
+ * SwimmerArray.cu:173,179; the stream is keyed by (seed, swimmer, step). */
+int lbswim_rng_draws(unsigned long long seed, int n, unsigned long long step, float* uniform,
+                     double* normal);
 
 /* ---- TracerArray (TracerArray.cu, TracerArray.h) --------------------------- */
 /* TracerArray::TracerArray(n), TracerArray.cu:5-10. */

@@ -17,6 +17,15 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
 
 
+def rel_l2_maxnorm(a, b):
+    """RMS of a - b over max |b|: relative L2 of a field normalised by its
+    largest magnitude, for fields such as u that are ~0 in places."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    mb = np.max(np.abs(b))
+    return float(np.sqrt(np.mean((a - b) ** 2)) / (mb if mb > 0 else 1.0))
+
+
 def rel_max(a, b):
     """max |a - b| / max |b| (for fields such as u that are ~0 in places)."""
     a = np.asarray(a, dtype=np.float64)
