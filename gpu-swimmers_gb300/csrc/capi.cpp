@@ -404,6 +404,20 @@ int lbswim_rng_draws(unsigned long long seed, int n, unsigned long long step, fl
   API_END
 }
 
+int lbswim_spread_forces_noalloc(const double* r, const double* n, int nsw, double P, double l,
+                                 int nx, int ny, int nz, double* force, int accumulate,
+                                 void* stream) {
+  API_BEGIN
+  REQUIRE(nsw >= 0, "swimmer count must be non-negative");
+  REQUIRE(nsw == 0 || (r && n), "position or orientation pointer is NULL");
+  REQUIRE(force, "force pointer is NULL");
+  REQUIRE(nx > 0 && ny > 0 && nz > 0 && nx <= 65535, "bad lattice dimensions");
+  REQUIRE(std::isfinite(P) && std::isfinite(l), "P and l must be finite");
+  const int size[3] = {nx, ny, nz};
+  spread_forces_noalloc(r, n, nsw, P, l, size, force, accumulate, (cudaStream_t)stream);
+  API_END
+}
+
 // ---- TracerArray -----------------------------------------------------------------
 int lbswim_tracers_create(int n, lbswim_tracers** out) {
   API_BEGIN

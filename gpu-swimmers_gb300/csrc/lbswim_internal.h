@@ -122,5 +122,8 @@ void tracers_move(Tracers* T, Lattice* L);
 void lattice_interp_velocity(Lattice* L, int npoints, const double* r_host, double* v_host);
 void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,
                double* g_host);
+void spread_forces_noalloc(const double* r, const double* nv, int nsw, double P, double l,
+                           const int size[3], double* force, int accumulate,
+                           cudaStream_t stream);
 
 }  // namespace lbswim

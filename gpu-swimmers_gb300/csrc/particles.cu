@@ -8,6 +8,8 @@
 // gathers the ends whose stencil covers it in a fixed (bin, end) order before
 // one write of its force.  No floating-point atomics are used.
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "lbswim_device.cuh"
 #include "lbswim_internal.h"
@@ -511,6 +513,91 @@ void lattice_interp_velocity(Lattice* L, int np, const double* r_host, double* v
   }
   cudaFree(r);
   cudaFree(v);
+}
+
+// ---- allocation-free spreading ------------------------------------------------
+// Scratch of lbswim_spread_forces_noalloc: one file-scope device array that
+// every GPU loading the library holds until exit.  Layout (bytes):
+//   bin counts [NOALLOC_MAX_BINS] | bin starts [NOALLOC_MAX_BINS + 1] |
+//   scan tile sums | end order [NOALLOC_MAX_ENDS] | end records [NOALLOC_MAX_ENDS]
+constexpr int NOALLOC_MAX_ENDS = 2 * LBSWIM_NOALLOC_MAX_SWIMMERS;
+constexpr int NOALLOC_MAX_BINS = LBSWIM_NOALLOC_MAX_SPREAD_BINS;
+constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t NA_COUNT = 0;
+constexpr size_t NA_START = NA_COUNT + align256(sizeof(unsigned) * NOALLOC_MAX_BINS);
+constexpr size_t NA_TILES = NA_START + align256(sizeof(unsigned) * (NOALLOC_MAX_BINS + 1));
+constexpr size_t NA_ORDER =
+    NA_TILES + align256(sizeof(unsigned) * ((NOALLOC_MAX_BINS + SCAN_TILE - 1) / SCAN_TILE));
+constexpr size_t NA_ENDS = NA_ORDER + align256(sizeof(int) * NOALLOC_MAX_ENDS);
+constexpr size_t NA_BYTES = NA_ENDS + align256(sizeof(EndRecord<double>) * NOALLOC_MAX_ENDS);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (the symbol's name in host code is only a stand-in).
+static unsigned char* noalloc_scratch_for_current_device() {
+  static std::mutex mu;
+  static unsigned char* addr[64] = {nullptr};
+  int dev = 0;
+  LB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw LbswimError{LBSWIM_ENOTSUP, "device index out of range"};
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    LB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = (unsigned char*)p;
+  }
+  return addr[dev];
+}
+
+void spread_forces_noalloc(const double* r, const double* nv, int nsw, double P, double l,
+                           const int size[3], double* force, int accumulate,
+                           cudaStream_t stream) {
+  Dims D;
+  for (int a = 0; a < 3; ++a) {
+    D.n[a] = size[a];
+    D.nb[a] = (size[a] + BIN - 1) / BIN;
+  }
+  D.N = (long long)size[0] * size[1] * size[2];
+  const long long nbins = (long long)D.nb[0] * D.nb[1] * D.nb[2];
+  const int nends = 2 * nsw;
+  if (nends > NOALLOC_MAX_ENDS)
+    throw LbswimError{LBSWIM_EINVAL, "more swimmers than the allocation-free limit of " +
+                                         std::to_string(LBSWIM_NOALLOC_MAX_SWIMMERS)};
+  if (nbins > NOALLOC_MAX_BINS)
+    throw LbswimError{LBSWIM_EINVAL,
+                      "lattice larger than the allocation-free limit (" +
+                          std::to_string(NOALLOC_MAX_BINS) + " spread bins of 4^3 sites)"};
+  unsigned char* base = noalloc_scratch_for_current_device();
+  unsigned* bin_count = (unsigned*)(base + NA_COUNT);
+  unsigned* bin_start = (unsigned*)(base + NA_START);
+  unsigned* tiles = (unsigned*)(base + NA_TILES);
+  int* order = (int*)(base + NA_ORDER);
+  EndRecord<double>* ends = (EndRecord<double>*)(base + NA_ENDS);
+  // The array keeps the previous call's contents: the counts must start at zero.
+  LB_CUDA(cudaMemsetAsync(bin_count, 0, sizeof(unsigned) * nbins, stream));
+  const int nb = (int)nbins;
+  if (nends > 0) {
+    k_spread_bin<double><<<(nends + 255) / 256, 256, 0, stream>>>(nsw, r, nv, P, l, D, ends,
+                                                                  bin_count);
+    LB_CHECK_LAUNCH(1);
+  }
+  const int ntiles = (nb + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_tiles<<<ntiles, SCAN_THREADS, 0, stream>>>(bin_count, nb, tiles);
+  k_scan_top<<<1, 1024, 0, stream>>>(tiles, ntiles);
+  k_scan_apply<<<ntiles, SCAN_THREADS, 0, stream>>>(bin_count, nb, tiles, bin_start,
+                                                    (unsigned)nends);
+  LB_CHECK_LAUNCH(3);
+  if (nends > 0) {
+    k_spread_scatter<double><<<(nends + 255) / 256, 256, 0, stream>>>(nends, ends, D, bin_count,
+                                                                      bin_start, order);
+    k_spread_sort<<<(nb + 255) / 256, 256, 0, stream>>>(nb, bin_start, order);
+    LB_CHECK_LAUNCH(2);
+  }
+  dim3 grid((D.n[2] + 31) / 32, (D.n[1] + 7) / 8, D.n[0]);
+  k_spread_gather<double><<<grid, dim3(32, 8), 0, stream>>>(D, ends, bin_start, order, force,
+                                                            accumulate);
+  LB_CHECK_LAUNCH(1);
 }
 
 void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,

@@ -91,6 +91,8 @@ _PROTOS = {
     "lbswim_lattice_interp_velocity": (C.c_int, [_VP, C.c_int, _D, _D]),
     "lbswim_rng_draws": (C.c_int, [C.c_ulonglong, C.c_int, C.c_ulonglong,
                                    C.POINTER(C.c_float), _D]),
+    "lbswim_spread_forces_noalloc": (C.c_int, [_VP, _VP, C.c_int, C.c_double, C.c_double,
+                                               C.c_int, C.c_int, C.c_int, _VP, C.c_int, _VP]),
     "lbswim_tracers_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "lbswim_tracers_destroy": (C.c_int, [_VP]),
     "lbswim_tracers_get_num": (C.c_int, [_VP, C.POINTER(C.c_int)]),

@@ -188,6 +188,36 @@ int lbswim_lattice_interp_velocity(lbswim_lattice* lat, int npoints, const doubl
 int lbswim_rng_draws(unsigned long long seed, int n, unsigned long long step, float* uniform,
                      double* normal);
 
+/* ---- allocation-free force spreading --------------------------------------- */
+/* Limits of lbswim_spread_forces_noalloc's built-in scratch (about 6.5 MB of
+ * device memory, held by every GPU that loads the library until exit). */
+#define LBSWIM_NOALLOC_MAX_SWIMMERS 16384
+#define LBSWIM_NOALLOC_MAX_SPREAD_BINS 262144 /* 4x4x4-site bins: up to 256^3 */
+
+/* No counterpart in the reference: it always allocates through SharedArray.
+ * Spreads the dipole forces of nsw swimmers (the computation of
+ * lbswim_swimmers_add_forces) into a caller-owned FP64 force field without
+ * allocating any memory, for callers that cannot call cudaMalloc: code running
+ * inside CUDA stream capture, real-time loops where an allocation's implicit
+ * synchronisation or failure is not acceptable, and hosts that own all device
+ * memory through their own allocator.
+ * All pointers are device pointers owned by the caller: r and n are the
+ * swimmers' positions and orientations, [3][nsw] doubles; force is
+ * [3][nx*ny*nz] doubles, overwritten (accumulate = 0) or added to
+ * (accumulate != 0).  Work is enqueued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream).  Scratch lives in one static device array:
+ * nsw may be at most LBSWIM_NOALLOC_MAX_SWIMMERS and the lattice at most
+ * LBSWIM_NOALLOC_MAX_SPREAD_BINS spread bins (ceil(nx/4)*ceil(ny/4)*ceil(nz/4));
+ * larger inputs are rejected with LBSWIM_EINVAL before any work is enqueued.
+ * The first call on a device looks up the array's device address (with that
+ * device current), so make that first call before any stream capture begins.
+ * All calls on a device share the one scratch array: calls whose work
+ * overlaps on the GPU (different streams, or concurrent host threads) race and
+ * give wrong results; serialise them on one stream. */
+int lbswim_spread_forces_noalloc(const double* r, const double* n, int nsw, double P, double l,
+                                 int nx, int ny, int nz, double* force, int accumulate,
+                                 void* stream);
+
 /* ---- TracerArray (TracerArray.cu, TracerArray.h) --------------------------- */
 /* TracerArray::TracerArray(n), TracerArray.cu:5-10. */
 int lbswim_tracers_create(int n, lbswim_tracers** out);
