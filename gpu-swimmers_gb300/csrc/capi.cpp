@@ -127,9 +127,7 @@ int lbswim_lattice_zero_force(lbswim_lattice* lat) {
   check_lattice(lat);
   // Deferred: the next consumer of the force either overwrites it (spreading)
   // or treats it as zero; a read of the field clears the buffer first.
-  Lattice* L = LAT(lat);
-  L->force_zero_pending = true;
-  L->force_version++;
+  lattice_zero_force(LAT(lat));
   API_END
 }
 
@@ -227,16 +225,18 @@ int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, 
   REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
   Lattice* L = const_cast<Lattice*>(CLAT(lat));
   if (field == LBSWIM_FIELD_FORCE) lattice_materialise_force(L);
+  const bool packed = L->precision != LBSWIM_F64;
   switch (field) {
-    case LBSWIM_FIELD_RHO: *ptr = L->rho; break;
-    case LBSWIM_FIELD_U: *ptr = L->u; break;
+    case LBSWIM_FIELD_RHO: *ptr = packed ? (void*)L->hydro : L->rho; break;
+    case LBSWIM_FIELD_U: *ptr = packed ? (void*)L->hydro : L->u; break;
     case LBSWIM_FIELD_FORCE: *ptr = L->force; break;
     case LBSWIM_FIELD_FOLD: *ptr = L->f[L->cur]; break;
     default: *ptr = L->f[L->cur ^ 1]; break;
   }
   if (elem) {
     const bool is_f = field == LBSWIM_FIELD_FOLD || field == LBSWIM_FIELD_FNEW;
-    *elem = is_f ? elem_bytes(L->precision) : (L->precision == LBSWIM_F64 ? 8 : 4);
+    const bool is_h = field == LBSWIM_FIELD_RHO || field == LBSWIM_FIELD_U;
+    *elem = is_f ? elem_bytes(L->precision) : (packed ? (is_h ? 16 : 4) : 8);
   }
   API_END
 }
@@ -427,17 +427,9 @@ int lbswim_tracers_create(int n, lbswim_tracers** out) {
   Tracers* T = new Tracers();
   T->n = n;
   try {
-    const size_t bytes = sizeof(double) * 3 * (size_t)(n > 0 ? n : 1);
-    LB_CUDA(cudaMalloc(&T->r, bytes));
-    LB_CUDA(cudaMalloc(&T->s, bytes));
-    LB_CUDA(cudaMalloc(&T->v, bytes));
-    LB_CUDA(cudaMemset(T->r, 0, bytes));
-    LB_CUDA(cudaMemset(T->s, 0, bytes));
-    LB_CUDA(cudaMemset(T->v, 0, bytes));
+    tracers_alloc(T);
   } catch (...) {
-    cudaFree(T->r);
-    cudaFree(T->s);
-    cudaFree(T->v);
+    tracers_free(T);
     delete T;
     throw;
   }
@@ -452,9 +444,7 @@ int lbswim_tracers_destroy(lbswim_tracers* tr) {
   if (!tr) return LBSWIM_OK;
   Tracers* T = TR(tr);
   cudaDeviceSynchronize();
-  cudaFree(T->r);
-  cudaFree(T->s);
-  cudaFree(T->v);
+  tracers_free(T);
   delete T;
   API_END
 }
@@ -474,26 +464,19 @@ int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat) {
   API_END
 }
 
-static double* tr_field(Tracers* T, int field) {
-  REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
-  return field == LBSWIM_TR_R ? T->r : (field == LBSWIM_TR_S ? T->s : T->v);
-}
-
 int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host) {
   API_BEGIN
   REQUIRE(tr && host, "NULL argument");
-  Tracers* T = TR(tr);
-  LB_CUDA(cudaDeviceSynchronize());
-  LB_CUDA(cudaMemcpy(tr_field(T, field), host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+  REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
+  tracers_h2d(TR(tr), field, host);
   API_END
 }
 
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host) {
   API_BEGIN
   REQUIRE(tr && host, "NULL argument");
-  Tracers* T = TR(tr);
-  LB_CUDA(cudaDeviceSynchronize());
-  LB_CUDA(cudaMemcpy(host, tr_field(T, field), sizeof(double) * 3 * T->n, cudaMemcpyDeviceToHost));
+  REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
+  tracers_d2h(TR(tr), field, host);
   API_END
 }
 
@@ -509,8 +492,7 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
   for (int i = 0; i < n_tracers; ++i) REQUIRE(tracers[i], "tracer handle is NULL");
   Lattice* L = LAT(lat);
   for (int t = 0; t < nsteps; ++t) {
-    L->force_zero_pending = true;  // ZeroForce
-    L->force_version++;
+    lattice_zero_force(L);  // ZeroForce
     for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
     lattice_step(L);
     lattice_calc_hydro(L);

@@ -180,17 +180,71 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
 }
 
 // Equilibrium from rho, u, lb.cu:314-371 (compat_sxz reproduces lb.cu:356).
-template <class S, class H>
-__global__ void k_init_from_hydro(const H* __restrict__ rho, const H* __restrict__ u,
-                                  S* __restrict__ f, long long N, double rho0, int compat_sxz) {
+// rho, u come from the FP64 SoA fields or, when packed is set, the float4 ones.
+template <class S>
+__global__ void k_init_from_hydro(const double* __restrict__ rho, const double* __restrict__ u,
+                                  const float4* __restrict__ packed, S* __restrict__ f,
+                                  long long N, double rho0, int compat_sxz) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
-    const double r = rho[s], ux = u[s], uy = u[N + s], uz = u[2 * N + s];
+    double r, ux, uy, uz;
+    if (packed) {
+      const float4 h = packed[s];
+      r = h.w;
+      ux = h.x;
+      uy = h.y;
+      uz = h.z;
+    } else {
+      r = rho[s];
+      ux = u[s];
+      uy = u[N + s];
+      uz = u[2 * N + s];
+    }
     double out[15];
     project<double>(r - rho0, r * ux, r * uy, r * uz, r * ux * ux, r * uy * uy, r * uz * uz,
                     r * ux * uy, compat_sxz ? r * ux * uy : r * ux * uz, r * uy * uz, out);
 #pragma unroll
-    for (int p = 0; p < 15; ++p) Store<S>::st(f + p * N + s, (S)stored_from_dev<S>(out[p], p));
+    for (int p = 0; p < 15; ++p) Store<S>::st(f + p * N + s, stored_from_dev<S>(out[p], p));
+  }
+}
+
+// rho, u from the stored distributions and the force into the packed fields
+// (CalcHydro of a reduced-precision lattice when the step's result is stale).
+template <class S>
+__global__ void k_calc_hydro_packed(const S* __restrict__ f, const float* __restrict__ F,
+                                    float4* __restrict__ hydro, long long N, float rho0) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
+       s += (long long)gridDim.x * blockDim.x) {
+    float d[15];
+#pragma unroll
+    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((float)Store<S>::ld(f + p * N + s), p);
+    float R, jx, jy, jz;
+    hydro_moments(d, R, jx, jy, jz);
+    float fx, fy, fz;
+    load_force(F, N, s, fx, fy, fz);
+    const float r = rho0 + R;
+    const float inv = 1.0f / r;
+    hydro[s] = make_float4((jx + 0.5f * fx) * inv, (jy + 0.5f * fy) * inv, (jz + 0.5f * fz) * inv, r);
+  }
+}
+
+// Host FP64 [components][N] <-> packed float4 component c (0-2: u, 3: rho).
+__global__ void k_packed_from_f64(const double* __restrict__ src, float* __restrict__ packed,
+                                  long long off, long long cnt, long long N, int rho_field) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long e = off + i;
+    const int c = rho_field ? 3 : (int)(e / N);
+    packed[4 * (e % N) + c] = (float)src[i];
+  }
+}
+__global__ void k_packed_to_f64(const float* __restrict__ packed, double* __restrict__ dst,
+                                long long off, long long cnt, long long N, int rho_field) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long e = off + i;
+    const int c = rho_field ? 3 : (int)(e / N);
+    dst[i] = (double)packed[4 * (e % N) + c];
   }
 }
 
@@ -241,29 +295,50 @@ __global__ void k_f32_to_f64(const float* __restrict__ src, double* __restrict__
 // ---------------------------------------------------------------------------
 constexpr int FUSED_LX = 32;
 constexpr int FUSED_RING_THREADS = 96;
+constexpr int SPREAD_CAP = 256;  // ends of one slab held in shared memory
 
 struct FusedArgs {
   const void* f_old;
   void* f_new;
-  const float* force;  // null: zero force
-  float* rho;
-  float* u;
+  const float* force;  // dense force base; null: zero
+  float4* hydro;  // {ux, uy, uz, rho} per site
   int nx, ny, nz;
   long long n;
   float rho0;
   Relax<float> k;
+  // pending dipole ends spread by the kernel itself (SPREAD instances)
+  const EndRecord<float>* ends;
+  const unsigned* slab_start;
+  const int* slab_list;
+  const float* fixed_scale;  // device: 2^S, 2^-S of the fixed-point force sums
 };
 
-template <int TZ, int TY>
+// Post-collision populations wait in shared memory until the output plane can
+// pull them: those moving +x (1, 7-10) are read two planes later, those at rest
+// in x (0, 3-6) one plane later, those moving -x (2, 11-14) in the same plane.
+// With one barrier per plane that needs 4, 3 and 2 slots of 5 populations.
+__host__ __device__ constexpr int ring_group(int p) { return cx_of(p) > 0 ? 0 : (cx_of(p) == 0 ? 1 : 2); }
+__host__ __device__ constexpr int ring_index(int p) {
+  return p == 1 || p == 0 || p == 2 ? 0 : (p <= 6 ? p - 2 : (p <= 10 ? p - 6 : p - 10));
+}
+constexpr int RING_POP_PLANES = 5 * (4 + 3 + 2);
+
+template <int TZ, int TY, bool SPREAD>
 constexpr int fused_smem_bytes() {
-  return 4 * 15 * (TY + 2) * (TZ + 2) * (int)sizeof(float);
+  return RING_POP_PLANES * (TY + 2) * (TZ + 2) * (int)sizeof(float) +
+         (SPREAD ? SPREAD_CAP * ((int)sizeof(EndRecord<float>) + 8) +
+                       2 * 3 * (TY + 2) * (TZ + 2) * (int)sizeof(long long)
+                 : 0);
 }
 
-template <class S, int TZ, int TY>
+template <class S, int TZ, int TY, bool SPREAD>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
   constexpr int NI = TY * TZ;
-  constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ, SLOT = 15 * PLANE;
-  extern __shared__ float sm[];
+  constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
+  extern __shared__ __align__(16) float sm[];
+  float* ringA = sm;                     // [4][5][PLANE]
+  float* ringB = ringA + 4 * 5 * PLANE;  // [3][5][PLANE]
+  float* ringC = ringB + 3 * 5 * PLANE;  // [2][5][PLANE]
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * FUSED_LX;
@@ -296,6 +371,71 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   const long long yz = (long long)gy * nz + gz;
   const S* __restrict__ fo = (const S*)a.f_old;
   const float* __restrict__ F = a.force;
+  const int my = ly * HZ + lz;
+
+  // ---- this slab's pending dipole ends and the fixed-point force planes ----
+  EndRecord<float>* srec = reinterpret_cast<EndRecord<float>*>(sm + RING_POP_PLANES * PLANE);
+  long long* fq = reinterpret_cast<long long*>(srec + SPREAD_CAP);  // [2][3][PLANE]
+  // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 64
+  unsigned long long* xmask = reinterpret_cast<unsigned long long*>(fq + 2 * 3 * PLANE);
+  const float fx_scale = SPREAD ? a.fixed_scale[0] : 0.f;
+  const float fx_inv = SPREAD ? a.fixed_scale[1] : 0.f;
+  int cnt = 0;
+  unsigned s0 = 0;
+  bool in_smem = true;
+  if (SPREAD) {
+    const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    s0 = a.slab_start[slab];
+    cnt = (int)(a.slab_start[slab + 1] - s0);
+    in_smem = cnt <= SPREAD_CAP;
+    if (in_smem) {
+      for (int q = tid; q < cnt; q += blockDim.x) {
+        srec[q] = a.ends[a.slab_list[s0 + q]];
+        unsigned long long m = 0ull;
+        float w;
+        for (int kk = 0; kk < ex + 2; ++kk)
+          if (cover_weight(wrap_once(x0 - 1 + kk, nx), srec[q].o[0], nx, srec[q].phi[0], w))
+            m |= 1ull << kk;
+        xmask[q] = m;
+      }
+    }
+    for (int i = tid; i < 2 * 3 * PLANE; i += blockDim.x) fq[i] = 0;
+    __syncthreads();
+  }
+  auto rec = [&](int q) -> const EndRecord<float>& {
+    return in_smem ? srec[q] : a.ends[a.slab_list[s0 + q]];
+  };
+  // Add every end-node contribution of local plane kk into fq[buf]: the pairs
+  // (end, (jy, jz) node) are shared among all threads of the CTA.
+  auto scatter_plane = [&](int kk, int buf) {
+    const int gx = wrap_once(x0 - 1 + kk, nx);
+    long long* f0 = fq + buf * 3 * PLANE;
+    for (int t = tid; t < cnt * 16; t += blockDim.x) {
+      if (in_smem && !((xmask[t >> 4] >> kk) & 1ull)) continue;
+      const EndRecord<float>& e = rec(t >> 4);
+      float wx;
+      if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
+      const int jy = (t >> 2) & 3, jz = t & 3;
+      const float py = e.phi[1][jy], pz = e.phi[2][jz];
+      const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+      const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+      const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+      // every local copy of the node's site in the halo-inclusive cross-section
+      const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
+      for (int ly2 = wrap_any(yg - y0 + 1, ny); ly2 <= ey + 1; ly2 += ny)
+        for (int lz2 = wrap_any(zg - z0 + 1, nz); lz2 <= ez + 1; lz2 += nz) {
+          const int at = ly2 * HZ + lz2;
+          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + at), (unsigned long long)q0);
+          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + PLANE + at), (unsigned long long)q1);
+          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + 2 * PLANE + at),
+                    (unsigned long long)q2);
+        }
+    }
+  };
+  if (SPREAD) {
+    scatter_plane(0, 0);
+    __syncthreads();
+  }
 
   float pre[18];
   auto load = [&](int gx) {
@@ -313,32 +453,46 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   if (active) load(wrap_once(x0 - 1, nx));
 
   float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f;
-  const int my = ly * HZ + lz;
+  int k3 = 0;  // k % 3
   for (int k = 0; k < ex + 2; ++k) {
     float cur[18];
 #pragma unroll
     for (int i = 0; i < 18; ++i) cur[i] = pre[i];
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
+    if (SPREAD && active) {
+      // force = base + spread (k_force_tile writes the same bits)
+      long long* f0 = fq + (k & 1) * 3 * PLANE + my;
+      cur[15] += fx_value(f0[0], fx_inv);
+      cur[16] += fx_value(f0[PLANE], fx_inv);
+      cur[17] += fx_value(f0[2 * PLANE], fx_inv);
+      f0[0] = f0[PLANE] = f0[2 * PLANE] = 0;  // ready for plane k + 2
+    }
     if (active) {
       float d[15];
 #pragma unroll
       for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>(cur[p], p);
       collide(d, cur[15], cur[16], cur[17], a.rho0, a.k, d);
-      float* slot = sm + (k & 3) * SLOT + my;
+      float* wa = ringA + (k & 3) * 5 * PLANE + my;
+      float* wb = ringB + k3 * 5 * PLANE + my;
+      float* wc = ringC + (k & 1) * 5 * PLANE + my;
 #pragma unroll
-      for (int p = 0; p < 15; ++p) slot[p * PLANE] = d[p];
+      for (int p = 0; p < 15; ++p) {
+        float* w = ring_group(p) == 0 ? wa : (ring_group(p) == 1 ? wb : wc);
+        w[ring_index(p) * PLANE] = d[p];
+      }
     }
+    if (SPREAD && k + 1 < ex + 2) scatter_plane(k + 1, (k + 1) & 1);
     __syncthreads();
     if (k >= 2 && interior) {
       const long long s = (long long)(x0 + k - 2) * nynz + yz;
-      const float* sm_m = sm + ((k - 2) & 3) * SLOT + my;  // plane x-1: c_x = +1
-      const float* sm_0 = sm + ((k - 1) & 3) * SLOT + my;  // plane x:   c_x = 0
-      const float* sm_p = sm + (k & 3) * SLOT + my;        // plane x+1: c_x = -1
+      const float* ra = ringA + ((k - 2) & 3) * 5 * PLANE + my;  // plane x-1: c_x = +1
+      const float* rb = ringB + (k3 == 0 ? 2 : k3 - 1) * 5 * PLANE + my;  // plane x
+      const float* rc = ringC + (k & 1) * 5 * PLANE + my;  // plane x+1: c_x = -1
       float g[15];
 #pragma unroll
       for (int p = 0; p < 15; ++p) {
-        const int off = p * PLANE - cy_of(p) * HZ - cz_of(p);
-        g[p] = cx_of(p) > 0 ? sm_m[off] : (cx_of(p) < 0 ? sm_p[off] : sm_0[off]);
+        const int off = ring_index(p) * PLANE - cy_of(p) * HZ - cz_of(p);
+        g[p] = ring_group(p) == 0 ? ra[off] : (ring_group(p) == 1 ? rb[off] : rc[off]);
       }
       float R, jx, jy, jz;
       hydro_moments(g, R, jx, jy, jz);
@@ -347,14 +501,13 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
       for (int p = 0; p < 15; ++p) Store<S>::st(fn + p * N + s, stored_from_dev<S>(g[p], p));
       const float rho = a.rho0 + R;
       const float inv = 1.0f / rho;
-      a.rho[s] = rho;
-      a.u[s] = (jx + 0.5f * Fp0) * inv;
-      a.u[N + s] = (jy + 0.5f * Fp1) * inv;
-      a.u[2 * N + s] = (jz + 0.5f * Fp2) * inv;
+      a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
+                               (jz + 0.5f * Fp2) * inv, rho);
     }
     Fp0 = cur[15];
     Fp1 = cur[16];
     Fp2 = cur[17];
+    k3 = k3 == 2 ? 0 : k3 + 1;
   }
 }
 
@@ -378,27 +531,29 @@ void lattice_alloc(Lattice* L) {
   const size_t he = L->precision == LBSWIM_F64 ? 8 : 4;
   L->f[0] = dmalloc(15 * N * fe);
   L->f[1] = dmalloc(15 * N * fe);
-  L->rho = dmalloc(N * he);
-  L->u = dmalloc(3 * N * he);
-  L->force = dmalloc(3 * N * he);
-  if (L->precision != LBSWIM_F64) {
-    L->rho_shadow = dmalloc(N * he);
-    L->u_shadow = dmalloc(3 * N * he);
+  if (L->precision == LBSWIM_F64) {
+    L->rho = dmalloc(N * he);
+    L->u = dmalloc(3 * N * he);
+    LB_CUDA(cudaMemsetAsync(L->rho, 0, N * he, L->stream));
+    LB_CUDA(cudaMemsetAsync(L->u, 0, 3 * N * he, L->stream));
+  } else {
+    L->hydro = (float4*)dmalloc(N * sizeof(float4));
+    L->hydro_shadow = (float4*)dmalloc(N * sizeof(float4));
+    LB_CUDA(cudaMemsetAsync(L->hydro, 0, N * sizeof(float4), L->stream));
   }
+  L->force = dmalloc(3 * N * he);
   // Contents start at zero so that reading a field before setting it is defined.
-  LB_CUDA(cudaMemsetAsync(L->rho, 0, N * he, L->stream));
-  LB_CUDA(cudaMemsetAsync(L->u, 0, 3 * N * he, L->stream));
   LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * N * he, L->stream));
   LB_CUDA(cudaMemsetAsync(L->f[0], 0, 15 * N * fe, L->stream));
   LB_CUDA(cudaMemsetAsync(L->f[1], 0, 15 * N * fe, L->stream));
 }
 
 void lattice_free(Lattice* L) {
-  void* ptrs[] = {L->f[0], L->f[1], L->rho, L->u, L->rho_shadow, L->u_shadow, L->force,
-                  L->staging, L->spread.bin_count, L->spread.bin_start, L->spread.scan_tmp,
-                  L->spread.order, L->spread.ends};
+  void* ptrs[] = {L->f[0], L->f[1], L->rho, L->u, L->hydro, L->hydro_shadow, L->force,
+                  L->staging};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  spread_free(L->spread);
   for (auto& p : L->timed) {
     cudaEventDestroy(p.first);
     cudaEventDestroy(p.second);
@@ -429,8 +584,13 @@ void lattice_zero_force_now(Lattice* L) {
   L->force_zero_pending = false;
 }
 
-void lattice_materialise_force(Lattice* L) {
-  if (L->force_zero_pending) lattice_zero_force_now(L);
+void lattice_materialise_force(Lattice* L) { spread_materialise(L); }
+
+void lattice_zero_force(Lattice* L) {
+  L->force_zero_pending = true;
+  L->spread.pending = 0;
+  L->spread.stepped = false;
+  L->force_version++;
 }
 
 template <class S>
@@ -438,11 +598,11 @@ static void init_from_hydro_t(Lattice* L) {
   const long long N = L->n;
   const int compat = (L->compat & LBSWIM_COMPAT_INIT_SXZ) ? 1 : 0;
   if (L->precision == LBSWIM_F64)
-    k_init_from_hydro<S, double><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        (const double*)L->rho, (const double*)L->u, (S*)L->f[L->cur], N, 0.0, compat);
+    k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const double*)L->rho, (const double*)L->u, nullptr, (S*)L->f[L->cur], N, 0.0, compat);
   else
-    k_init_from_hydro<S, float><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        (const float*)L->rho, (const float*)L->u, (S*)L->f[L->cur], N, L->rho0, compat);
+    k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        nullptr, nullptr, L->hydro, (S*)L->f[L->cur], N, L->rho0, compat);
   LB_CHECK_LAUNCH(1);
 }
 
@@ -456,28 +616,41 @@ void lattice_init_from_hydro(Lattice* L) {
   L->f_version++;
 }
 
-template <class S, int TZ, int TY>
+template <class S, int TZ, int TY, bool SPREAD>
 static void launch_fused(Lattice* L, const FusedArgs& a) {
-  constexpr int smem = fused_smem_bytes<TZ, TY>();
+  constexpr int smem = fused_smem_bytes<TZ, TY, SPREAD>();
   static bool configured = false;  // per template instance, per process
   if (!configured) {
-    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY>,
+    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     configured = true;
   }
   dim3 grid((a.nz + TZ - 1) / TZ, (a.ny + TY - 1) / TY, (a.nx + FUSED_LX - 1) / FUSED_LX);
-  k_fused_step<S, TZ, TY><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
+  k_fused_step<S, TZ, TY, SPREAD><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
   LB_CHECK_LAUNCH(1);
+}
+
+template <class S, int TZ, int TY>
+static void fused_step_tile(Lattice* L, FusedArgs& a) {
+  if (L->spread.pending > 0) {
+    const SlabSpread sp = spread_prepare_slabs(L, FUSED_LX, TY, TZ);
+    a.ends = (const EndRecord<float>*)sp.ends;
+    a.slab_start = sp.start;
+    a.slab_list = sp.list;
+    a.fixed_scale = sp.fixed_scale;
+    launch_fused<S, TZ, TY, true>(L, a);
+  } else {
+    launch_fused<S, TZ, TY, false>(L, a);
+  }
 }
 
 template <class S>
 static void fused_step_t(Lattice* L) {
-  FusedArgs a;
+  FusedArgs a{};
   a.f_old = L->f[L->cur];
   a.f_new = L->f[L->cur ^ 1];
   a.force = L->force_zero_pending ? nullptr : (const float*)L->force;
-  a.rho = (float*)L->rho_shadow;
-  a.u = (float*)L->u_shadow;
+  a.hydro = L->hydro_shadow;
   a.nx = L->size[0];
   a.ny = L->size[1];
   a.nz = L->size[2];
@@ -485,9 +658,9 @@ static void fused_step_t(Lattice* L) {
   a.rho0 = (float)L->rho0;
   a.k = make_relax<float>(L->tau_s, L->tau_b);
   if (L->fused_tile == 1)
-    launch_fused<S, 16, 16>(L, a);
+    fused_step_tile<S, 16, 16>(L, a);
   else
-    launch_fused<S, 32, 8>(L, a);
+    fused_step_tile<S, 32, 8>(L, a);
 }
 
 static std::pair<cudaEvent_t, cudaEvent_t> timing_pair(Lattice* L) {
@@ -540,6 +713,7 @@ void lattice_step(Lattice* L) {
     LB_CUDA(cudaEventRecord(ev.second, L->stream));
     L->timed.push_back(ev);
   }
+  if (L->precision != LBSWIM_F64 && L->spread.pending > 0) L->spread.stepped = true;
   L->cur ^= 1;
   L->f_version++;
   if (L->precision != LBSWIM_F64) {
@@ -550,12 +724,17 @@ void lattice_step(Lattice* L) {
   if (L->compat & LBSWIM_COMPAT_SYNC_STEP) LB_CUDA(cudaStreamSynchronize(L->stream));
 }
 
-template <class S, class H>
+template <class S>
 static void calc_hydro_t(Lattice* L) {
   const long long N = L->n;
-  k_calc_hydro<S, H><<<grid_for(N, 256), 256, 0, L->stream>>>(
-      (const S*)L->f[L->cur], L->force_zero_pending ? nullptr : (const H*)L->force, (H*)L->rho,
-      (H*)L->u, N, (H)L->rho0);
+  if (L->precision == LBSWIM_F64)
+    k_calc_hydro<double, double><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const double*)L->f[L->cur], L->force_zero_pending ? nullptr : (const double*)L->force,
+        (double*)L->rho, (double*)L->u, N, 0.0);
+  else
+    k_calc_hydro_packed<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const S*)L->f[L->cur], L->force_zero_pending ? nullptr : (const float*)L->force,
+        L->hydro, N, (float)L->rho0);
   LB_CHECK_LAUNCH(1);
 }
 
@@ -563,16 +742,16 @@ void lattice_calc_hydro(Lattice* L) {
   if (L->precision != LBSWIM_F64 && L->shadow_f_version == L->f_version &&
       L->shadow_force_version == L->force_version) {
     // The last Step already produced rho, u for this fOld and this force.
-    std::swap(L->rho, L->rho_shadow);
-    std::swap(L->u, L->u_shadow);
+    std::swap(L->hydro, L->hydro_shadow);
     L->shadow_f_version = 0;
     return;
   }
+  lattice_materialise_force(L);
   switch (L->precision) {
-    case LBSWIM_F64: calc_hydro_t<double, double>(L); break;
-    case LBSWIM_F32: calc_hydro_t<float, float>(L); break;
-    case LBSWIM_BF16: calc_hydro_t<__nv_bfloat16, float>(L); break;
-    default: calc_hydro_t<__half, float>(L); break;
+    case LBSWIM_F64: calc_hydro_t<double>(L); break;
+    case LBSWIM_F32: calc_hydro_t<float>(L); break;
+    case LBSWIM_BF16: calc_hydro_t<__nv_bfloat16>(L); break;
+    default: calc_hydro_t<__half>(L); break;
   }
 }
 
@@ -614,8 +793,8 @@ static void f_d2h_t(Lattice* L, const void* src, double* host) {
 
 static void* field_ptr(Lattice* L, int field) {
   switch (field) {
-    case LBSWIM_FIELD_RHO: return L->rho;
-    case LBSWIM_FIELD_U: return L->u;
+    case LBSWIM_FIELD_RHO: return L->precision == LBSWIM_F64 ? L->rho : (void*)L->hydro;
+    case LBSWIM_FIELD_U: return L->precision == LBSWIM_F64 ? L->u : (void*)L->hydro;
     case LBSWIM_FIELD_FORCE: return L->force;
     case LBSWIM_FIELD_FOLD: return L->f[L->cur];
     default: return L->f[L->cur ^ 1];
@@ -627,6 +806,8 @@ void lattice_h2d(Lattice* L, int field, const double* host) {
   void* dst = field_ptr(L, field);
   if (field == LBSWIM_FIELD_FORCE) {
     L->force_zero_pending = false;
+    L->spread.pending = 0;
+    L->spread.stepped = false;
     L->force_version++;
   }
   if (field == LBSWIM_FIELD_FOLD) L->f_version++;
@@ -648,7 +829,11 @@ void lattice_h2d(Lattice* L, int field, const double* host) {
       const long long c = std::min(chunk, cnt - off);
       LB_CUDA(cudaMemcpyAsync(st, host + off, c * sizeof(double), cudaMemcpyHostToDevice,
                               L->stream));
-      k_f64_to_f32<<<grid_for(c, 256), 256, 0, L->stream>>>(st, (float*)dst + off, c);
+      if (field == LBSWIM_FIELD_FORCE)
+        k_f64_to_f32<<<grid_for(c, 256), 256, 0, L->stream>>>(st, (float*)dst + off, c);
+      else
+        k_packed_from_f64<<<grid_for(c, 256), 256, 0, L->stream>>>(
+            st, (float*)L->hydro, off, c, L->n, field == LBSWIM_FIELD_RHO);
       LB_CHECK_LAUNCH(1);
     }
   }
@@ -676,7 +861,11 @@ void lattice_d2h(Lattice* L, int field, double* host) {
   double* st = staging(L, chunk);
   for (long long off = 0; off < cnt; off += chunk) {
     const long long c = std::min(chunk, cnt - off);
-    k_f32_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>((const float*)src + off, st, c);
+    if (field == LBSWIM_FIELD_FORCE)
+      k_f32_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>((const float*)src + off, st, c);
+    else
+      k_packed_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>(
+          (const float*)L->hydro, st, off, c, L->n, field == LBSWIM_FIELD_RHO);
     LB_CHECK_LAUNCH(1);
     LB_CUDA(cudaMemcpyAsync(host + off, st, c * sizeof(double), cudaMemcpyDeviceToHost,
                             L->stream));

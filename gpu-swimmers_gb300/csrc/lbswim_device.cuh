@@ -270,4 +270,106 @@ __device__ __forceinline__ void rng_normal3(uint64_t seed, uint32_t swimmer, uin
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+__device__ __forceinline__ int wrap_any(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// ---- dipole ends of the force spreading (SwimmerArray.cu:42-112) ---------------
+template <class T>
+struct EndRecord {
+  int o[3];  // wrapped stencil origin ceil(r - 2)
+  int pad;
+  T phi[3][4];  // Peskin weights of the 4 stencil nodes per axis
+  T F[3];       // force carried by the end
+};
+
+// Weight of one axis: sum of phi[i] over stencil nodes (o + i) mod n equal to x.
+template <class T>
+__device__ __forceinline__ T axis_weight(int x, int o, int n, const T phi[4]) {
+  if (n >= 4) {
+    int d = x - o;
+    if (d < 0) d += n;
+    return d <= 3 ? phi[d] : T(0);
+  }
+  T w = T(0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if ((o + i) % n == x) w += phi[i];
+  return w;
+}
+
+// Does the stencil of an end with origin o cover coordinate x on an axis of n
+// sites, and with which summed weight (n < 4 folds several nodes onto x)?
+template <class T>
+__device__ __forceinline__ bool cover_weight(int x, int o, int n, const T phi[4], T& w) {
+  if (n >= 4) {
+    int d = x - o;
+    if (d < 0) d += n;
+    if (d > 3) return false;
+    w = phi[d];
+    return true;
+  }
+  w = axis_weight(x, o, n, phi);
+  return true;
+}
+
+// cover_weight with the four weights in a float4 (kept in registers); same
+// selection and, for n < 4, the same summation order.
+__device__ __forceinline__ float pick4(const float4& p, int i) {
+  return i == 0 ? p.x : (i == 1 ? p.y : (i == 2 ? p.z : p.w));
+}
+__device__ __forceinline__ bool cover_weight4(int x, int o, int n, const float4& p, float& w) {
+  if (n >= 4) {
+    int d = x - o;
+    if (d < 0) d += n;
+    if (d > 3) return false;
+    w = pick4(p, d);
+    return true;
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if ((o + i) % n == x) s += pick4(p, i);
+  w = s;
+  return true;
+}
+
+// One end's contribution to one force component at a site.  FP64 keeps the
+// reference's order ((phi_x phi_y) phi_z) F (SwimmerArray.cu:64-73); FP32
+// evaluates (phi_y phi_z)(phi_x F) so that phi_x F can be formed once per x
+// plane.  Every FP32 kernel that spreads uses this one expression, so the
+// step kernel's own spreading and the materialised force agree bit for bit.
+__device__ __forceinline__ double end_contrib(double wx, double wy, double wz, double F) {
+  return (wx * wy * wz) * F;
+}
+__device__ __forceinline__ float end_contrib_f(float wy, float wz, float wxF) {
+  return (wy * wz) * wxF;
+}
+
+// ---- fixed-point force accumulation (FP32 lattices) ---------------------------
+// Each end-node contribution c = (phi_y phi_z)(phi_x F) is quantised to
+// round(c 2^S) and summed in 64-bit integers.  Integer sums are exact, so the
+// force is the same whatever order the contributions arrive in: shared-memory
+// atomics in the step kernel and the gather of k_force_tile give identical
+// bits.  The host picks S so that the sum of all |c| stays below 2^62.
+__device__ __forceinline__ long long fx_quant(float c, float scale) {
+  return __float2ll_rn(c * scale);
+}
+__device__ __forceinline__ float fx_value(long long q, float inv_scale) {
+  return __ll2float_rn(q) * inv_scale;
+}
+__device__ __forceinline__ float node_contrib(float py, float pz, float wx, float F) {
+  return (py * pz) * (wx * F);
+}
+
+// Rank of key k among the cnt distinct keys: its position in increasing order.
+__device__ __forceinline__ int rank_of(int k, const int* keys, int cnt) {
+  int r = 0;
+  for (int j = 0; j < cnt; ++j) r += keys[j] < k;
+  return r;
+}
+
+
+
 }  // namespace lbswim

@@ -41,17 +41,42 @@ inline int elem_bytes(int precision) {
   return precision == LBSWIM_F64 ? 8 : precision == LBSWIM_F32 ? 4 : 2;
 }
 
-// Device scratch for deterministic force spreading: dipole ends binned by the
-// 4x4x4 block of their stencil origin.
+// Dipole ends listed under every tile their stencil touches (one set of lists
+// per tiling).
+struct TileLists {
+  int ntiles = 0;
+  unsigned* count = nullptr;     // [ntiles], zero between uses
+  unsigned* start = nullptr;     // [ntiles + 1]
+  unsigned* scan_tmp = nullptr;  // block sums for the scan
+  int* list = nullptr;           // [capacity] end ids grouped by tile
+  int* sorted = nullptr;         // [capacity] ordered copy for oversized tiles
+  long long capacity = 0;
+};
+
+// Force spreading state.  The lattice force is base + the spread of the
+// `pending` dipole ends recorded since the base was set (base = zero after
+// ZeroForce, else the dense force buffer).  FP64 lattices fold the ends into
+// the dense buffer at once; reduced-precision lattices keep them pending and
+// the step kernel spreads them itself, so the force never goes through HBM
+// unless someone reads it.
 struct SpreadScratch {
   int capacity_ends = 0;
-  int nbins = 0;
-  unsigned* bin_count = nullptr;  // [nbins], zero between calls
-  unsigned* bin_start = nullptr;  // [nbins + 1]
-  unsigned* scan_tmp = nullptr;   // block sums for the scan
-  int* order = nullptr;           // [capacity_ends] end ids grouped by bin
-  void* ends = nullptr;           // [capacity_ends] EndRecord
+  void* ends = nullptr;  // [capacity_ends] EndRecord of the pending ends
   size_t ends_bytes = 0;
+  int pending = 0;
+  bool stepped = false;  // a Step already consumed the pending ends
+  unsigned* max_abs_force = nullptr;  // device: largest |F| component of the pending ends
+  float* fixed_scale = nullptr;       // device: 2^S and 2^-S of the fixed-point sums
+  TileLists ftiles;      // force tiles, for materialisation
+  TileLists slabs;       // step-kernel slabs
+};
+
+// What the fused step kernel needs to spread the pending ends itself.
+struct SlabSpread {
+  const void* ends = nullptr;
+  const unsigned* start = nullptr;
+  const int* list = nullptr;
+  const float* fixed_scale = nullptr;
 };
 
 struct Lattice {
@@ -63,10 +88,12 @@ struct Lattice {
   lbswim_lbparams params;
   void* f[2] = {nullptr, nullptr};  // f[cur] is fOld
   int cur = 0;
-  void* rho = nullptr;  // double (F64) or float
-  void* u = nullptr;
-  void* rho_shadow = nullptr;  // rho/u of the post-Step state, written by the fused kernel
-  void* u_shadow = nullptr;
+  void* rho = nullptr;  // FP64 lattices: double[N]
+  void* u = nullptr;    // FP64 lattices: double[3][N]
+  // FP32/BF16/FP16 lattices: rho and u packed per site as float4 {ux, uy, uz, rho};
+  // the shadow holds the post-Step state the fused kernel writes.
+  float4* hydro = nullptr;
+  float4* hydro_shadow = nullptr;
   void* force = nullptr;
   cudaStream_t stream = 0;
   int time_step = 0;
@@ -95,11 +122,30 @@ struct Swimmers {
   double* nv = nullptr;
 };
 
+// Tracers live on the device in a work order binned by position (8^3-site
+// bins, re-binned every TRACER_RESORT_MOVES moves and after positions are
+// uploaded) so that neighbouring threads read neighbouring velocities.
+// perm[k] is the user index of work slot k.
+constexpr int TRACER_RESORT_MOVES = 64;
 struct Tracers {
   int n;
-  double* r = nullptr;
+  double* r = nullptr;  // [3][n] work order
   double* s = nullptr;
   double* v = nullptr;
+  double* r2 = nullptr;  // re-binning targets
+  double* s2 = nullptr;
+  double* v2 = nullptr;
+  int* perm = nullptr;
+  int* perm2 = nullptr;
+  int* bin_of = nullptr;
+  double* staging = nullptr;  // [3][n] user order, for H2D / D2H
+  bool identity = true;       // perm is the identity
+  bool needs_sort = true;
+  int moves_since_sort = 0;
+  int nbins = 0;
+  unsigned* bin_count = nullptr;
+  unsigned* bin_start = nullptr;
+  unsigned* scan_tmp = nullptr;
 };
 
 // lattice.cu
@@ -114,11 +160,21 @@ void lattice_h2d(Lattice* L, int field, const double* host);
 void lattice_d2h(Lattice* L, int field, double* host);
 void fill_params(lbswim_lbparams* p, double tau_s, double tau_b);
 void lattice_read_timing(Lattice* L, double* total_ms, int* launches);
+void lattice_zero_force(Lattice* L);
+
+// particles.cu: force spreading state
+void spread_materialise(Lattice* L);
+SlabSpread spread_prepare_slabs(Lattice* L, int LX, int TY, int TZ);
+void spread_free(SpreadScratch& S);
 
 // particles.cu
 void swimmers_add_forces(Swimmers* S, Lattice* L);
 void swimmers_move(Swimmers* S, Lattice* L);
 void tracers_move(Tracers* T, Lattice* L);
+void tracers_alloc(Tracers* T);
+void tracers_free(Tracers* T);
+void tracers_h2d(Tracers* T, int field, const double* host);
+void tracers_d2h(Tracers* T, int field, double* host);
 void lattice_interp_velocity(Lattice* L, int npoints, const double* r_host, double* v_host);
 void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,
                double* g_host);

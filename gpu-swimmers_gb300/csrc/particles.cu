@@ -3,10 +3,16 @@
 // Spreading (reference SwimmerArray.cu:42-121) adds, for each swimmer, -P n at
 // the tail r - l n and +P n at the head r through the 4^3 Peskin stencil.  The
 // reference scatters with FP64 atomics in arbitrary order.  Here the result is
-// deterministic: the 2n dipole ends are binned by the 4x4x4 block holding
-// their stencil origin, each bin is put in end order, and every lattice site
-// gathers the ends whose stencil covers it in a fixed (bin, end) order before
-// one write of its force.  No floating-point atomics are used.
+// deterministic and uses no floating-point atomics: AddForces records the 2n
+// dipole ends (origin, Peskin weights, force); the ends are then listed under
+// every tile their stencil touches (integer counting sort), and each tile sums,
+// for every site, the covering ends in end order.  The tiles are either force
+// tiles (k_force_tile, which writes the dense force field) or, for FP32/BF16/
+// FP16 lattices, the slabs of the fused step kernel, which spreads the ends
+// itself so the force field never goes through HBM.
+//
+// The original 4^3-origin-bin kernels below (k_spread_bin ... k_spread_gather)
+// serve lbswim_spread_forces_noalloc.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -18,24 +24,11 @@ namespace lbswim {
 
 constexpr int BIN = 4;  // spread bin edge, in lattice sites
 
-template <class T>
-struct EndRecord {
-  int o[3];  // wrapped stencil origin ceil(r - 2)
-  int pad;
-  T phi[3][4];  // Peskin weights of the 4 stencil nodes per axis
-  T F[3];       // force carried by the end
-};
-
 struct Dims {
   int n[3];
   int nb[3];  // bins per axis
   long long N;
 };
-
-__device__ __forceinline__ int wrap_any(int i, int n) {
-  i %= n;
-  return i < 0 ? i + n : i;
-}
 
 template <class T>
 __device__ __forceinline__ void stencil_setup(const Dims& D, const double r[3], int o[3],
@@ -101,21 +94,6 @@ __global__ void k_spread_sort(int nbins, const unsigned* __restrict__ bin_start,
     }
     order[j] = v;
   }
-}
-
-// Weight of one axis: sum of phi[i] over stencil nodes (o + i) mod n equal to x.
-template <class T>
-__device__ __forceinline__ T axis_weight(int x, int o, int n, const T phi[4]) {
-  if (n >= 4) {
-    int d = x - o;
-    if (d < 0) d += n;
-    return d <= 3 ? phi[d] : T(0);
-  }
-  T w = T(0);
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-    if ((o + i) % n == x) w += phi[i];
-  return w;
 }
 
 __device__ __forceinline__ int candidate_bins(int x, int n, int out[4]) {
@@ -261,13 +239,274 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const unsigned* __r
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = grand_total;
 }
 
+// ---- tile-touch spreading ------------------------------------------------------
+// Every dipole end is listed under each force tile its stencil touches; a tile's
+// list is then put in end order, and one CTA per tile sums, for each of its
+// sites, the covering ends of its list in that order.  The per-site order is a
+// fixed function of the input, so the result is deterministic.
+struct TileGrid {
+  int T[3];   // tile edge per axis
+  int h;      // sites beyond the tile (every side) that also need the force
+  int nt[3];  // tiles per axis
+};
+
+// Tiles along one axis whose extended region holds one of the nodes o..o+3:
+// the sites o-h .. o+3+h form one cyclic interval, so the tiles form the cyclic
+// range first, first+1, ... (count of them, at most nt).  An interval that
+// wraps past the end covers the tiles from `first` to the last one and from 0
+// to the tile of its wrapped end; if those meet, it covers every tile.
+__device__ __forceinline__ void touched_range(int o, int n, int T, int h, int nt, int& first,
+                                              int& count) {
+  const int len = 4 + 2 * h;
+  if (len >= n) {
+    first = 0;
+    count = nt;
+    return;
+  }
+  const int a = wrap_any(o - h, n), b = a + len - 1;
+  first = a / T;
+  if (b < n) {
+    count = b / T - first + 1;
+  } else {
+    const int last = (b - n) / T;
+    count = last >= first ? nt : (nt - first) + last + 1;
+  }
+}
+
+constexpr int REC_THREADS = 256;
+
+// One record per dipole end: e = 2i is the tail, 2i + 1 the head.  Records are
+// assembled in shared memory and written out as one contiguous block.
+template <class T>
+__global__ void __launch_bounds__(REC_THREADS) k_end_records(int nsw, const double* __restrict__ r,
+                                                             const double* __restrict__ nv,
+                                                             double P, double l, Dims D,
+                                                             EndRecord<T>* __restrict__ ends,
+                                                             unsigned* __restrict__ max_abs_f) {
+  __shared__ EndRecord<T> srec[REC_THREADS];
+  __shared__ unsigned smax;
+  if (threadIdx.x == 0) smax = 0u;
+  __syncthreads();
+  const int e0 = blockIdx.x * REC_THREADS;
+  const int e = e0 + threadIdx.x;
+  const int nends = 2 * nsw;
+  if (e < nends) {
+    const int i = e >> 1;
+    const bool head = e & 1;
+    double rr[3], F[3];
+    for (int a = 0; a < 3; ++a) {
+      const double na = nv[nsw * a + i];
+      rr[a] = head ? r[nsw * a + i] : r[nsw * a + i] - na * l;
+      F[a] = -P * na;
+      if (head) F[a] *= -1.0;
+    }
+    EndRecord<T>& rec = srec[threadIdx.x];
+    stencil_setup<T>(D, rr, rec.o, rec.phi);
+    rec.pad = 0;
+    float m = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      rec.F[a] = (T)F[a];
+      m = fmaxf(m, fabsf((float)F[a]));
+    }
+    // non-negative floats order like their bit patterns
+    atomicMax(&smax, __float_as_uint(m));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && max_abs_f) atomicMax(max_abs_f, smax);
+  const int nrec = min(REC_THREADS, nends - e0);
+  const int words = nrec * (int)(sizeof(EndRecord<T>) / 4);
+  const unsigned* src = reinterpret_cast<const unsigned*>(srec);
+  unsigned* dst = reinterpret_cast<unsigned*>(ends + e0);
+  for (int w = threadIdx.x; w < words; w += REC_THREADS) dst[w] = src[w];
+}
+
+// pass 0 counts, pass 1 scatters end ids into the tile lists.
+template <class T, int PASS>
+__global__ void k_touch(int nends, const EndRecord<T>* __restrict__ ends, Dims D, TileGrid G,
+                        unsigned* __restrict__ count, const unsigned* __restrict__ start,
+                        int* __restrict__ list) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nends) return;
+  const int ox = ends[e].o[0], oy = ends[e].o[1], oz = ends[e].o[2];
+  int fx, cx, fy, cy, fz, cz;
+  touched_range(ox, D.n[0], G.T[0], G.h, G.nt[0], fx, cx);
+  touched_range(oy, D.n[1], G.T[1], G.h, G.nt[1], fy, cy);
+  touched_range(oz, D.n[2], G.T[2], G.h, G.nt[2], fz, cz);
+  for (int i = 0; i < cx; ++i) {
+    const int kx = fx + i < G.nt[0] ? fx + i : fx + i - G.nt[0];
+    for (int j = 0; j < cy; ++j) {
+      const int ky = fy + j < G.nt[1] ? fy + j : fy + j - G.nt[1];
+      for (int k = 0; k < cz; ++k) {
+        const int kz = fz + k < G.nt[2] ? fz + k : fz + k - G.nt[2];
+        const int t = (kx * G.nt[1] + ky) * G.nt[2] + kz;
+        if (PASS == 0) {
+          atomicAdd(count + t, 1u);
+        } else {
+          // counting back down leaves the counts at zero for the next call
+          const unsigned slot = atomicSub(count + t, 1u) - 1u;
+          list[start[t] + slot] = e;
+        }
+      }
+    }
+  }
+}
+
+// Exclusive-scan finish that also writes the grand total to out[n].
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply_total(
+    const unsigned* __restrict__ in, int n, const unsigned* __restrict__ tile_off,
+    unsigned* __restrict__ out) {
+  __shared__ unsigned ws[32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+  unsigned v[SCAN_PER_THREAD];
+  unsigned s = 0;
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    v[i] = base + i < n ? in[base + i] : 0u;
+    s += v[i];
+  }
+  unsigned total;
+  unsigned run = block_exclusive_scan(s, ws, total) + tile_off[blockIdx.x];
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+    if (base + i == n - 1) out[n] = run;
+  }
+}
+
+// 2^S with S the largest power keeping every fixed-point site sum below 2^61: a
+// site's contributions add up to at most (number of ends) x (largest |F|).
+__global__ void k_fx_scale(int npending, const unsigned* __restrict__ max_abs_f,
+                           float* __restrict__ out) {
+  const float m = __uint_as_float(*max_abs_f);
+  int S = 60;
+  if (m > 0.f && npending > 0) {
+    const double bound = (double)npending * (double)m * 1.0000001;
+    S = (int)floor(61.0 - log2(bound));
+  }
+  S = max(-100, min(100, S));
+  out[0] = ldexpf(1.0f, S);
+  out[1] = ldexpf(1.0f, -S);
+}
+
+// Force tile: 8 (x) x 8 (y) x 32 (z) sites, 16 warps, each warp owns 4 of the 64
+// z-rows; a warp ballot picks the ends covering a row.
+//  * FP64: the ends are put in end order by rank and every site adds their
+//    contributions in that order, ((phi_x phi_y) phi_z) F as the reference
+//    does (SwimmerArray.cu:64-73).
+//  * FP32: every end-node contribution is quantised and summed in 64-bit
+//    fixed point, exactly as the step kernel's own spreading does.
+constexpr int FT_X = 8, FT_Y = 8, FT_Z = 32, FT_THREADS = 512, FT_CAP = 256;
+
+template <class T>
+__global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
+                                                           const EndRecord<T>* __restrict__ ends,
+                                                           const unsigned* __restrict__ start,
+                                                           const int* __restrict__ list,
+                                                           int* __restrict__ sorted,
+                                                           const float* __restrict__ fixed_scale,
+                                                           T* __restrict__ force, int accumulate) {
+  constexpr bool FIXED = sizeof(T) == 4;
+  __shared__ EndRecord<T> srec[FT_CAP];
+  __shared__ int skey[FT_CAP];
+  const int tile = blockIdx.x;
+  const int kz = tile % G.nt[2], ky = (tile / G.nt[2]) % G.nt[1], kx = tile / (G.nt[1] * G.nt[2]);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const unsigned s0 = start[tile], s1 = start[tile + 1];
+  const int cnt = (int)(s1 - s0);
+  const bool in_smem = cnt <= FT_CAP;
+  if (in_smem) {
+    if (FIXED) {
+      for (int q = tid; q < cnt; q += FT_THREADS) srec[q] = ends[list[s0 + q]];
+    } else {
+      for (int q = tid; q < cnt; q += FT_THREADS) skey[q] = list[s0 + q];
+      __syncthreads();
+      for (int q = tid; q < cnt; q += FT_THREADS) srec[rank_of(skey[q], skey, cnt)] = ends[skey[q]];
+    }
+  } else if (!FIXED) {
+    // more ends than fit: order them in global scratch and read records from there
+    for (int q = tid; q < cnt; q += FT_THREADS) {
+      const int k = list[s0 + q];
+      int r = 0;
+      for (int j = 0; j < cnt; ++j) r += list[s0 + j] < k;
+      sorted[s0 + r] = k;
+    }
+  }
+  __syncthreads();
+  auto rec = [&](int q) -> const EndRecord<T>& {
+    return in_smem ? srec[q] : ends[FIXED ? list[s0 + q] : sorted[s0 + q]];
+  };
+  const float fx_scale = FIXED ? fixed_scale[0] : 0.f, fx_inv = FIXED ? fixed_scale[1] : 0.f;
+  const int z = kz * FT_Z + lane;
+  const bool zval = z < D.n[2];
+  for (int row = warp; row < FT_X * FT_Y; row += FT_THREADS / 32) {
+    const int x = kx * FT_X + (row >> 3), y = ky * FT_Y + (row & 7);
+    if (x >= D.n[0] || y >= D.n[1]) continue;
+    T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+    long long q0 = 0, q1 = 0, q2 = 0;
+    bool hit = false;
+    for (int base = 0; base < cnt; base += 32) {
+      const int q = base + lane;
+      bool covers = false;
+      if (q < cnt) {
+        const EndRecord<T>& e = rec(q);
+        T w;
+        covers = cover_weight(x, e.o[0], D.n[0], e.phi[0], w) &&
+                 cover_weight(y, e.o[1], D.n[1], e.phi[1], w);
+      }
+      unsigned m = __ballot_sync(0xffffffffu, covers);
+      while (m) {
+        const int q2i = base + __ffs(m) - 1;
+        m &= m - 1;
+        const EndRecord<T>& e = rec(q2i);
+        T wx, wy, wz;
+        cover_weight(x, e.o[0], D.n[0], e.phi[0], wx);
+        if (!zval || !cover_weight(z, e.o[2], D.n[2], e.phi[2], wz)) continue;
+        hit = true;
+        if constexpr (FIXED) {
+          // per (jy, jz) node, as the step kernel scatters them
+          for (int jy = 0; jy < 4; ++jy) {
+            if (wrap_any(e.o[1] + jy, D.n[1]) != y) continue;
+            for (int jz = 0; jz < 4; ++jz) {
+              if (wrap_any(e.o[2] + jz, D.n[2]) != z) continue;
+              const float py = e.phi[1][jy], pz = e.phi[2][jz];
+              q0 += fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+              q1 += fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+              q2 += fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+            }
+          }
+        } else {
+          cover_weight(y, e.o[1], D.n[1], e.phi[1], wy);
+          acc0 += end_contrib(wx, wy, wz, e.F[0]);
+          acc1 += end_contrib(wx, wy, wz, e.F[1]);
+          acc2 += end_contrib(wx, wy, wz, e.F[2]);
+        }
+      }
+    }
+    if (!zval) continue;
+    const long long s = (long long)x * D.n[1] * D.n[2] + (long long)y * D.n[2] + z;
+    if constexpr (FIXED) {
+      // base + spread, the value the step kernel forms
+      const T b0 = accumulate ? force[s] : T(0), b1 = accumulate ? force[D.N + s] : T(0),
+              b2 = accumulate ? force[2 * D.N + s] : T(0);
+      force[s] = b0 + fx_value(q0, fx_inv);
+      force[D.N + s] = b1 + fx_value(q1, fx_inv);
+      force[2 * D.N + s] = b2 + fx_value(q2, fx_inv);
+    } else if (!accumulate) {
+      force[s] = acc0;
+      force[D.N + s] = acc1;
+      force[2 * D.N + s] = acc2;
+    } else if (hit) {
+      force[s] += acc0;
+      force[D.N + s] += acc1;
+      force[2 * D.N + s] += acc2;
+    }
+  }
+}
+
 // ---- Move kernels -----------------------------------------------------------
-// InterpVelocity, interp.cu:8-47: u at r through the 4^3 Peskin stencil.
-template <class U, class T>
-__device__ __forceinline__ void interp_velocity(const U* __restrict__ u, const Dims& D,
-                                                const double r[3], T v[3]) {
-  int idx[3][4];
-  T phi[3][4];
+// Stencil nodes and Peskin weights of position r (interp.cu:23-30).
+template <class T>
+__device__ __forceinline__ void interp_setup(const Dims& D, const double r[3], int idx[3][4],
+                                             T phi[3][4]) {
   for (int d = 0; d < 3; ++d) {
     const double x0 = ceil(r[d] - 2.);
     const int o = wrap_any((int)x0, D.n[d]);
@@ -279,6 +518,16 @@ __device__ __forceinline__ void interp_velocity(const U* __restrict__ u, const D
       phi[d][i] = peskin_delta<T>((T)(r[d] - (x0 + i)));
     }
   }
+}
+
+// InterpVelocity, interp.cu:8-47: u at r through the 4^3 Peskin stencil, from
+// the FP64 SoA field ...
+template <class T>
+__device__ __forceinline__ void interp_velocity(const double* __restrict__ u, const Dims& D,
+                                                const double r[3], T v[3]) {
+  int idx[3][4];
+  T phi[3][4];
+  interp_setup<T>(D, r, idx, phi);
   v[0] = v[1] = v[2] = T(0);
   const long long nynz = (long long)D.n[1] * D.n[2];
   for (int i = 0; i < 4; ++i)
@@ -292,6 +541,31 @@ __device__ __forceinline__ void interp_velocity(const U* __restrict__ u, const D
         v[0] += d3 * (T)u[s];
         v[1] += d3 * (T)u[D.N + s];
         v[2] += d3 * (T)u[2 * D.N + s];
+      }
+    }
+}
+
+// ... or from the packed float4 field of a reduced-precision lattice (one 16-byte
+// load per node).
+template <class T>
+__device__ __forceinline__ void interp_velocity(const float4* __restrict__ h, const Dims& D,
+                                                const double r[3], T v[3]) {
+  int idx[3][4];
+  T phi[3][4];
+  interp_setup<T>(D, r, idx, phi);
+  v[0] = v[1] = v[2] = T(0);
+  const long long nynz = (long long)D.n[1] * D.n[2];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      const T pij = phi[0][i] * phi[1][j];
+      const long long row = idx[0][i] * nynz + (long long)idx[1][j] * D.n[2];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const T d3 = pij * phi[2][k];
+        const float4 q = __ldg(h + row + idx[2][k]);
+        v[0] += d3 * (T)q.x;
+        v[1] += d3 * (T)q.y;
+        v[2] += d3 * (T)q.z;
       }
     }
 }
@@ -310,7 +584,7 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     n0[d] = swn[nsw * d + i];
   }
   T v[3];
-  interp_velocity<U, T>(u, D, r, v);
+  interp_velocity<T>(u, D, r, v);
   double rMinus[3];
   for (int d = 0; d < 3; ++d) {
     double rDot = c.mobility * c.P * n0[d];
@@ -325,7 +599,7 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     rng_normal3(seed, (uint32_t)i, step, nn);
   } else if (!c.rotational_advection_off) {  // rotate with the local shear
     T vm[3];
-    interp_velocity<U, T>(u, D, rMinus, vm);
+    interp_velocity<T>(u, D, rMinus, vm);
     for (int d = 0; d < 3; ++d) nn[d] = n0[d] + ((double)v[d] - (double)vm[d]) / c.l;
   } else {
     return;  // orientation unchanged
@@ -343,7 +617,7 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
   double rr[3];
   for (int d = 0; d < 3; ++d) rr[d] = r[ntr * d + i];
   T vv[3];
-  interp_velocity<U, T>(u, D, rr, vv);
+  interp_velocity<T>(u, D, rr, vv);
   for (int d = 0; d < 3; ++d) {
     const double vd = (double)vv[d];
     v[ntr * d + i] = vd;
@@ -359,7 +633,7 @@ __global__ void k_interp_points(int np, const double* __restrict__ r, double* __
   if (i >= np) return;
   const double rr[3] = {r[i], r[np + i], r[2 * np + i]};
   T vv[3];
-  interp_velocity<U, T>(u, D, rr, vv);
+  interp_velocity<T>(u, D, rr, vv);
   for (int d = 0; d < 3; ++d) v[np * d + i] = (double)vv[d];
 }
 
@@ -384,77 +658,206 @@ static Dims make_dims(const Lattice* L) {
   return D;
 }
 
-static void ensure_spread(Lattice* L, int nends) {
+static TileGrid force_tiles(const Lattice* L) {
+  TileGrid G;
+  G.T[0] = FT_X;
+  G.T[1] = FT_Y;
+  G.T[2] = FT_Z;
+  G.h = 0;
+  for (int a = 0; a < 3; ++a) G.nt[a] = (L->size[a] + G.T[a] - 1) / G.T[a];
+  return G;
+}
+
+// Upper bound on the tile-list entries of one end: 4 + 2h consecutive sites per
+// axis meet at most ceil((4 + 2h) / T) + 1 tiles, plus one more when they wrap
+// around a partial last tile.
+static long long touches_per_end(const TileGrid& G) {
+  long long m = 1;
+  for (int a = 0; a < 3; ++a)
+    m *= std::min<long long>(G.nt[a], (4 + 2 * G.h + G.T[a] - 1) / G.T[a] + 2);
+  return m;
+}
+
+static void free_lists(TileLists& TL) {
+  void* ptrs[] = {TL.count, TL.start, TL.scan_tmp, TL.list, TL.sorted};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  TL = TileLists();
+}
+
+void spread_free(SpreadScratch& S) {
+  if (S.ends) cudaFree(S.ends);
+  if (S.max_abs_force) cudaFree(S.max_abs_force);
+  if (S.fixed_scale) cudaFree(S.fixed_scale);
+  S.ends = nullptr;
+  S.max_abs_force = nullptr;
+  S.fixed_scale = nullptr;
+  free_lists(S.ftiles);
+  free_lists(S.slabs);
+}
+
+static size_t record_bytes(const Lattice* L) {
+  return L->precision == LBSWIM_F64 ? sizeof(EndRecord<double>) : sizeof(EndRecord<float>);
+}
+
+// Room for `total` pending ends, keeping the records already pending.
+static void ensure_ends(Lattice* L, int total) {
   SpreadScratch& S = L->spread;
-  const Dims D = make_dims(L);
-  const int nbins = D.nb[0] * D.nb[1] * D.nb[2];
-  if (S.nbins != nbins) {
-    if (S.bin_count) cudaFree(S.bin_count);
-    if (S.bin_start) cudaFree(S.bin_start);
-    if (S.scan_tmp) cudaFree(S.scan_tmp);
-    LB_CUDA(cudaMalloc(&S.bin_count, sizeof(unsigned) * nbins));
-    LB_CUDA(cudaMalloc(&S.bin_start, sizeof(unsigned) * (nbins + 1)));
-    const int ntiles = (nbins + SCAN_TILE - 1) / SCAN_TILE;
-    LB_CUDA(cudaMalloc(&S.scan_tmp, sizeof(unsigned) * std::max(ntiles, 1)));
-    LB_CUDA(cudaMemsetAsync(S.bin_count, 0, sizeof(unsigned) * nbins, L->stream));
-    S.nbins = nbins;
-  }
-  const size_t rec = L->precision == LBSWIM_F64 ? sizeof(EndRecord<double>) : sizeof(EndRecord<float>);
-  if (S.capacity_ends < nends || S.ends_bytes < rec * (size_t)nends) {
+  const size_t rec = record_bytes(L);
+  if (S.capacity_ends >= total && S.ends_bytes >= rec * (size_t)total) return;
+  const int cap = std::max(total + total / 2, 64);
+  void* fresh = nullptr;
+  LB_CUDA(cudaMalloc(&fresh, rec * cap));
+  if (S.ends && S.pending > 0)
+    LB_CUDA(cudaMemcpyAsync(fresh, S.ends, rec * S.pending, cudaMemcpyDeviceToDevice, L->stream));
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  if (S.ends) cudaFree(S.ends);
+  S.ends = fresh;
+  S.capacity_ends = cap;
+  S.ends_bytes = rec * cap;
+}
+
+static void ensure_lists(Lattice* L, TileLists& TL, const TileGrid& G, int nends) {
+  const int ntiles = G.nt[0] * G.nt[1] * G.nt[2];
+  if (TL.ntiles != ntiles) {
     LB_CUDA(cudaStreamSynchronize(L->stream));
-    if (S.order) cudaFree(S.order);
-    if (S.ends) cudaFree(S.ends);
-    const int cap = std::max(nends, 64);
-    LB_CUDA(cudaMalloc(&S.order, sizeof(int) * cap));
-    LB_CUDA(cudaMalloc(&S.ends, rec * cap));
-    S.capacity_ends = cap;
-    S.ends_bytes = rec * cap;
+    const long long keep = TL.capacity;
+    int* keep_list = TL.list;
+    int* keep_sorted = TL.sorted;
+    if (TL.count) cudaFree(TL.count);
+    if (TL.start) cudaFree(TL.start);
+    if (TL.scan_tmp) cudaFree(TL.scan_tmp);
+    TL.count = TL.start = TL.scan_tmp = nullptr;
+    LB_CUDA(cudaMalloc(&TL.count, sizeof(unsigned) * ntiles));
+    LB_CUDA(cudaMalloc(&TL.start, sizeof(unsigned) * (ntiles + 1)));
+    const int nscan = (ntiles + SCAN_TILE - 1) / SCAN_TILE;
+    LB_CUDA(cudaMalloc(&TL.scan_tmp, sizeof(unsigned) * std::max(nscan, 1)));
+    LB_CUDA(cudaMemsetAsync(TL.count, 0, sizeof(unsigned) * ntiles, L->stream));
+    TL.ntiles = ntiles;
+    TL.capacity = keep;
+    TL.list = keep_list;
+    TL.sorted = keep_sorted;
+  }
+  const long long need = std::max<long long>((long long)nends * touches_per_end(G), 64);
+  if (TL.capacity < need) {
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    if (TL.list) cudaFree(TL.list);
+    if (TL.sorted) cudaFree(TL.sorted);
+    TL.list = TL.sorted = nullptr;
+    LB_CUDA(cudaMalloc(&TL.list, sizeof(int) * need));
+    LB_CUDA(cudaMalloc(&TL.sorted, sizeof(int) * need));
+    TL.capacity = need;
   }
 }
 
-static void scan_bins(Lattice* L, unsigned total) {
-  SpreadScratch& S = L->spread;
-  const int ntiles = (S.nbins + SCAN_TILE - 1) / SCAN_TILE;
-  k_scan_tiles<<<ntiles, SCAN_THREADS, 0, L->stream>>>(S.bin_count, S.nbins, S.scan_tmp);
-  k_scan_top<<<1, 1024, 0, L->stream>>>(S.scan_tmp, ntiles);
-  k_scan_apply<<<ntiles, SCAN_THREADS, 0, L->stream>>>(S.bin_count, S.nbins, S.scan_tmp,
-                                                       S.bin_start, total);
+// Lists of the pending ends per tile of G (entries unordered within a tile).
+template <class T>
+static void bin_ends(Lattice* L, TileLists& TL, const TileGrid& G) {
+  const int nends = L->spread.pending;
+  ensure_lists(L, TL, G, nends);
+  const Dims D = make_dims(L);
+  const EndRecord<T>* ends = (const EndRecord<T>*)L->spread.ends;
+  if (nends > 0) {
+    k_touch<T, 0><<<(nends + 255) / 256, 256, 0, L->stream>>>(nends, ends, D, G, TL.count,
+                                                              nullptr, nullptr);
+    LB_CHECK_LAUNCH(1);
+  }
+  const int nscan = (TL.ntiles + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_tiles<<<nscan, SCAN_THREADS, 0, L->stream>>>(TL.count, TL.ntiles, TL.scan_tmp);
+  k_scan_top<<<1, 1024, 0, L->stream>>>(TL.scan_tmp, nscan);
+  k_scan_apply_total<<<nscan, SCAN_THREADS, 0, L->stream>>>(TL.count, TL.ntiles, TL.scan_tmp,
+                                                            TL.start);
   LB_CHECK_LAUNCH(3);
+  if (nends > 0) {
+    k_touch<T, 1><<<(nends + 255) / 256, 256, 0, L->stream>>>(nends, ends, D, G, TL.count,
+                                                              TL.start, TL.list);
+    LB_CHECK_LAUNCH(1);
+  }
+}
+
+// Fold the pending ends into the dense force buffer (force = base + spread).
+// 2^S for the fixed-point sums of the pending ends, computed on the device.
+static const float* fixed_scale_for_pending(Lattice* L) {
+  SpreadScratch& S = L->spread;
+  k_fx_scale<<<1, 1, 0, L->stream>>>(S.pending, S.max_abs_force, S.fixed_scale);
+  LB_CHECK_LAUNCH(1);
+  return S.fixed_scale;
 }
 
 template <class T>
-static void add_forces_t(Swimmers* W, Lattice* L) {
-  const int nends = 2 * W->n;
-  ensure_spread(L, nends);
+static void materialise_t(Lattice* L) {
   SpreadScratch& S = L->spread;
+  const TileGrid G = force_tiles(L);
+  bin_ends<T>(L, S.ftiles, G);
   const Dims D = make_dims(L);
-  EndRecord<T>* ends = (EndRecord<T>*)S.ends;
-  const int accumulate = L->force_zero_pending ? 0 : 1;
-  if (nends > 0) {
-    k_spread_bin<T><<<(nends + 255) / 256, 256, 0, L->stream>>>(
-        W->n, W->r, W->nv, W->common.P, W->common.l, D, ends, S.bin_count);
-    LB_CHECK_LAUNCH(1);
-  }
-  scan_bins(L, (unsigned)nends);
-  if (nends > 0) {
-    k_spread_scatter<T><<<(nends + 255) / 256, 256, 0, L->stream>>>(nends, ends, D, S.bin_count,
-                                                                     S.bin_start, S.order);
-    k_spread_sort<<<(S.nbins + 255) / 256, 256, 0, L->stream>>>(S.nbins, S.bin_start, S.order);
-    LB_CHECK_LAUNCH(2);
-  }
-  dim3 grid((D.n[2] + 31) / 32, (D.n[1] + 7) / 8, D.n[0]);
-  k_spread_gather<T><<<grid, dim3(32, 8), 0, L->stream>>>(D, ends, S.bin_start, S.order,
-                                                          (T*)L->force, accumulate);
+  const float* fs = sizeof(T) == 4 ? fixed_scale_for_pending(L) : nullptr;
+  k_force_tile<T><<<S.ftiles.ntiles, FT_THREADS, 0, L->stream>>>(
+      D, G, (const EndRecord<T>*)S.ends, S.ftiles.start, S.ftiles.list, S.ftiles.sorted, fs,
+      (T*)L->force, L->force_zero_pending ? 0 : 1);
   LB_CHECK_LAUNCH(1);
+  S.pending = 0;
+  S.stepped = false;
   L->force_zero_pending = false;
-  L->force_version++;
 }
 
+void spread_materialise(Lattice* L) {
+  if (L->spread.pending > 0) {
+    if (L->precision == LBSWIM_F64)
+      materialise_t<double>(L);
+    else
+      materialise_t<float>(L);
+  } else if (L->force_zero_pending) {
+    lattice_zero_force_now(L);
+  }
+}
+
+SlabSpread spread_prepare_slabs(Lattice* L, int LX, int TY, int TZ) {
+  SpreadScratch& S = L->spread;
+  TileGrid G;
+  G.T[0] = LX;
+  G.T[1] = TY;
+  G.T[2] = TZ;
+  G.h = 1;  // the step kernel collides a one-site ring around its slab
+  for (int a = 0; a < 3; ++a) G.nt[a] = (L->size[a] + G.T[a] - 1) / G.T[a];
+  bin_ends<float>(L, S.slabs, G);
+  SlabSpread out;
+  out.ends = S.ends;
+  out.start = S.slabs.start;
+  out.list = S.slabs.list;
+  out.fixed_scale = fixed_scale_for_pending(L);
+  return out;
+}
+
+template <class T>
+static void append_ends_t(Swimmers* W, Lattice* L) {
+  SpreadScratch& S = L->spread;
+  const int nends = 2 * W->n;
+  ensure_ends(L, S.pending + nends);
+  if (!S.max_abs_force) {
+    LB_CUDA(cudaMalloc(&S.max_abs_force, sizeof(unsigned)));
+    LB_CUDA(cudaMalloc(&S.fixed_scale, 2 * sizeof(float)));
+  }
+  if (S.pending == 0) LB_CUDA(cudaMemsetAsync(S.max_abs_force, 0, sizeof(unsigned), L->stream));
+  if (nends > 0) {
+    k_end_records<T><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
+        W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L),
+        (EndRecord<T>*)S.ends + S.pending, S.max_abs_force);
+    LB_CHECK_LAUNCH(1);
+  }
+  S.pending += nends;
+}
+
+// SwimmerArray::AddForces (SwimmerArray.cu:114-121).
 void swimmers_add_forces(Swimmers* W, Lattice* L) {
-  if (L->precision == LBSWIM_F64)
-    add_forces_t<double>(W, L);
-  else
-    add_forces_t<float>(W, L);
+  // ends already spread by a Step belong to the base from now on
+  if (L->spread.stepped) spread_materialise(L);
+  if (L->precision == LBSWIM_F64) {
+    append_ends_t<double>(W, L);
+    spread_materialise(L);
+  } else {
+    append_ends_t<float>(W, L);
+  }
+  L->force_version++;
 }
 
 void swimmers_move(Swimmers* W, Lattice* L) {
@@ -465,23 +868,168 @@ void swimmers_move(Swimmers* W, Lattice* L) {
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u);
     else
-      k_swimmers_move<float, float><<<grid, 256, 0, L->stream>>>(
-          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float*)L->u);
+      k_swimmers_move<float4, float><<<grid, 256, 0, L->stream>>>(
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     LB_CHECK_LAUNCH(1);
   }
   W->step++;
 }
 
+// ---- tracer work order ------------------------------------------------------------
+constexpr int TR_BIN = 8;
+
+__global__ void k_tr_bin(int n, const double* __restrict__ r, Dims D, int nb1, int nb2,
+                         int* __restrict__ bin_of, unsigned* __restrict__ count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int c[3];
+  for (int d = 0; d < 3; ++d) c[d] = wrap_any((int)floor(r[n * d + k]), D.n[d]) / TR_BIN;
+  const int b = (c[0] * nb1 + c[1]) * nb2 + c[2];
+  bin_of[k] = b;
+  atomicAdd(count + b, 1u);
+}
+
+__global__ void k_tr_permute(int n, const int* __restrict__ bin_of, unsigned* __restrict__ count,
+                             const unsigned* __restrict__ start, const double* __restrict__ r,
+                             const double* __restrict__ s, const double* __restrict__ v,
+                             const int* __restrict__ perm, double* __restrict__ r2,
+                             double* __restrict__ s2, double* __restrict__ v2,
+                             int* __restrict__ perm2) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int b = bin_of[k];
+  const unsigned slot = start[b] + atomicSub(count + b, 1u) - 1u;
+  for (int d = 0; d < 3; ++d) {
+    r2[(long long)n * d + slot] = r[(long long)n * d + k];
+    s2[(long long)n * d + slot] = s[(long long)n * d + k];
+    v2[(long long)n * d + slot] = v[(long long)n * d + k];
+  }
+  perm2[slot] = perm[k];
+}
+
+__global__ void k_iota(int n, int* __restrict__ p) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = k;
+}
+
+// dst[d][k] = src[d][perm[k]] (user order -> work order) or the inverse.
+template <bool TO_WORK>
+__global__ void k_tr_reorder(int n, const int* __restrict__ perm, const double* __restrict__ src,
+                             double* __restrict__ dst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int u = perm[k];
+  for (int d = 0; d < 3; ++d) {
+    if (TO_WORK)
+      dst[(long long)n * d + k] = src[(long long)n * d + u];
+    else
+      dst[(long long)n * d + u] = src[(long long)n * d + k];
+  }
+}
+
+void tracers_alloc(Tracers* T) {
+  const size_t n = (size_t)(T->n > 0 ? T->n : 1);
+  double** bufs[] = {&T->r, &T->s, &T->v, &T->r2, &T->s2, &T->v2, &T->staging};
+  for (double** b : bufs) {
+    LB_CUDA(cudaMalloc(b, sizeof(double) * 3 * n));
+    LB_CUDA(cudaMemset(*b, 0, sizeof(double) * 3 * n));
+  }
+  LB_CUDA(cudaMalloc(&T->perm, sizeof(int) * n));
+  LB_CUDA(cudaMalloc(&T->perm2, sizeof(int) * n));
+  LB_CUDA(cudaMalloc(&T->bin_of, sizeof(int) * n));
+  k_iota<<<(int)((n + 255) / 256), 256>>>((int)n, T->perm);
+  LB_CHECK_LAUNCH(1);
+  LB_CUDA(cudaDeviceSynchronize());
+}
+
+void tracers_free(Tracers* T) {
+  void* ptrs[] = {T->r,    T->s,      T->v,      T->r2,        T->s2,        T->v2,
+                  T->perm, T->perm2,  T->bin_of, T->staging,   T->bin_count, T->bin_start,
+                  T->scan_tmp};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+static double* tr_field_ptr(Tracers* T, int field) {
+  return field == LBSWIM_TR_R ? T->r : (field == LBSWIM_TR_S ? T->s : T->v);
+}
+
+void tracers_h2d(Tracers* T, int field, const double* host) {
+  LB_CUDA(cudaDeviceSynchronize());  // particle arrays are not bound to one stream
+  if (T->n <= 0) return;
+  double* dst = tr_field_ptr(T, field);
+  if (T->identity) {
+    LB_CUDA(cudaMemcpy(dst, host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+  } else {
+    LB_CUDA(cudaMemcpy(T->staging, host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+    k_tr_reorder<true><<<(T->n + 255) / 256, 256>>>(T->n, T->perm, T->staging, dst);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaDeviceSynchronize());
+  }
+  if (field == LBSWIM_TR_R) T->needs_sort = true;
+}
+
+void tracers_d2h(Tracers* T, int field, double* host) {
+  LB_CUDA(cudaDeviceSynchronize());
+  if (T->n <= 0) return;
+  const double* src = tr_field_ptr(T, field);
+  if (T->identity) {
+    LB_CUDA(cudaMemcpy(host, src, sizeof(double) * 3 * T->n, cudaMemcpyDeviceToHost));
+  } else {
+    k_tr_reorder<false><<<(T->n + 255) / 256, 256>>>(T->n, T->perm, src, T->staging);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaMemcpy(host, T->staging, sizeof(double) * 3 * T->n, cudaMemcpyDeviceToHost));
+  }
+}
+
+static void tracers_sort(Tracers* T, Lattice* L) {
+  const Dims D = make_dims(L);
+  const int nb0 = (D.n[0] + TR_BIN - 1) / TR_BIN, nb1 = (D.n[1] + TR_BIN - 1) / TR_BIN,
+            nb2 = (D.n[2] + TR_BIN - 1) / TR_BIN;
+  const int nbins = nb0 * nb1 * nb2;
+  if (T->nbins != nbins) {
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    if (T->bin_count) cudaFree(T->bin_count);
+    if (T->bin_start) cudaFree(T->bin_start);
+    if (T->scan_tmp) cudaFree(T->scan_tmp);
+    T->bin_count = T->bin_start = T->scan_tmp = nullptr;
+    LB_CUDA(cudaMalloc(&T->bin_count, sizeof(unsigned) * nbins));
+    LB_CUDA(cudaMalloc(&T->bin_start, sizeof(unsigned) * (nbins + 1)));
+    LB_CUDA(cudaMalloc(&T->scan_tmp, sizeof(unsigned) * ((nbins + SCAN_TILE - 1) / SCAN_TILE)));
+    LB_CUDA(cudaMemsetAsync(T->bin_count, 0, sizeof(unsigned) * nbins, L->stream));
+    T->nbins = nbins;
+  }
+  const int g = (T->n + 255) / 256;
+  k_tr_bin<<<g, 256, 0, L->stream>>>(T->n, T->r, D, nb1, nb2, T->bin_of, T->bin_count);
+  const int nscan = (nbins + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_tiles<<<nscan, SCAN_THREADS, 0, L->stream>>>(T->bin_count, nbins, T->scan_tmp);
+  k_scan_top<<<1, 1024, 0, L->stream>>>(T->scan_tmp, nscan);
+  k_scan_apply<<<nscan, SCAN_THREADS, 0, L->stream>>>(T->bin_count, nbins, T->scan_tmp,
+                                                      T->bin_start, (unsigned)T->n);
+  k_tr_permute<<<g, 256, 0, L->stream>>>(T->n, T->bin_of, T->bin_count, T->bin_start, T->r,
+                                         T->s, T->v, T->perm, T->r2, T->s2, T->v2, T->perm2);
+  LB_CHECK_LAUNCH(5);
+  std::swap(T->r, T->r2);
+  std::swap(T->s, T->s2);
+  std::swap(T->v, T->v2);
+  std::swap(T->perm, T->perm2);
+  T->identity = false;
+  T->needs_sort = false;
+  T->moves_since_sort = 0;
+}
+
 void tracers_move(Tracers* T, Lattice* L) {
   if (T->n <= 0) return;
+  if (T->needs_sort || T->moves_since_sort >= TRACER_RESORT_MOVES) tracers_sort(T, L);
+  T->moves_since_sort++;
   const Dims D = make_dims(L);
   const int grid = (T->n + 255) / 256;
   if (L->precision == LBSWIM_F64)
     k_tracers_move<double, double><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
                                                                  (const double*)L->u);
   else
-    k_tracers_move<float, float><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
-                                                               (const float*)L->u);
+    k_tracers_move<float4, float><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
+                                                                L->hydro);
   LB_CHECK_LAUNCH(1);
 }
 
@@ -501,8 +1049,8 @@ void lattice_interp_velocity(Lattice* L, int np, const double* r_host, double* v
       k_interp_points<double, double><<<(np + 255) / 256, 256, 0, L->stream>>>(np, r, v, D,
                                                                               (const double*)L->u);
     else
-      k_interp_points<float, float><<<(np + 255) / 256, 256, 0, L->stream>>>(np, r, v, D,
-                                                                            (const float*)L->u);
+      k_interp_points<float4, float><<<(np + 255) / 256, 256, 0, L->stream>>>(np, r, v, D,
+                                                                             L->hydro);
     LB_CHECK_LAUNCH(1);
     LB_CUDA(cudaMemcpyAsync(v_host, v, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, L->stream));
     LB_CUDA(cudaStreamSynchronize(L->stream));

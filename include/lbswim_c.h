@@ -144,7 +144,9 @@ int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out);
 int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags);
 int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
 int lbswim_lattice_synchronize(lbswim_lattice* lat);
-/* Device address and element size (8, 4 or 2) of a field's current buffer. */
+/* Device address and element size of a field's current buffer: 8 (FP64
+ * lattices); for FP32/BF16/FP16 lattices fOld/fNew are 4 or 2 bytes, force 4,
+ * and rho and u share one buffer of float4 {ux, uy, uz, rho} per site (16). */
 int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, int* elem_bytes);
 /* When enabled, every LB step kernel of this lattice is bracketed by CUDA
  * events on the lattice's stream.  get_timing synchronises the stream and

@@ -40,9 +40,9 @@ def test_f32_mass_conservation():
     assert abs(lat.fOld.data.sum() - m0) / m0 < 1e-7
 
 
-@pytest.mark.parametrize("shape", [(5, 7, 3), (17, 9, 33), (40, 3, 16), (1, 8, 8)])
+@pytest.mark.parametrize("shape", [(5, 7, 3), (17, 9, 33), (40, 3, 16), (1, 8, 8), (9, 7, 5), (33, 10, 40)])
 def test_f32_ragged_shapes_match_oracle(shape):
-    case = O.random_case(shape, 5, 20, seed=sum(shape), u_amp=0.01)
+    case = O.random_case(shape, 60, 20, seed=sum(shape), u_amp=0.01)
     lat, sw, tr, system = build_gpu(case, "f32")
     orc = O.make_system(case)
     system.Step(20)
@@ -51,3 +51,93 @@ def test_f32_ragged_shapes_match_oracle(shape):
     assert rel_l2(gs["rho"], os_["rho"]) < 1e-6
     assert rel_max(gs["u"], os_["u"]) < 1e-4
     assert rel_l2(gs["f"], os_["f"]) < 1e-6
+
+
+def _spread_case():
+    return O.random_case((40, 24, 36), 400, 300, seed=21, alpha=0.1, P=2e-3, l=0.4)
+
+
+@pytest.mark.parametrize("dense", [False, True])
+def test_f32_in_kernel_spread_equals_materialised_force(dense):
+    # (a) the step kernel spreads the pending ends itself; (b) the force is read
+    # back first, which writes the dense field, and the step then reads it.
+    # The dense case puts more ends on one slab and one plane than the kernel's
+    # shared-memory lists hold, which exercises its fallbacks.
+    case = (O.random_case((16, 16, 16), 600, 50, seed=3, alpha=0.1, P=2e-3, l=0.4) if dense
+            else _spread_case())
+    a = build_gpu(case, "f32")
+    b = build_gpu(case, "f32")
+    for t in range(6):
+        for lat, sw, tr, _ in (a, b):
+            lat.ZeroForce()
+            sw.AddForces(lat)
+        b[0].force.D2H()
+        for lat, sw, tr, _ in (a, b):
+            lat.Step()
+            lat.CalcHydro()
+            sw.Move(lat)
+            tr.Move(lat)
+    sa, sb = snapshot(*a[:3]), snapshot(*b[:3])
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_f32_force_matches_f64_force():
+    case = _spread_case()
+    l32 = build_gpu(case, "f32")
+    l64 = build_gpu(case, "f64")
+    for lat, sw, _, _ in (l32, l64):
+        lat.ZeroForce()
+        sw.AddForces(lat)
+        lat.force.D2H()
+    f32 = l32[0].force.data.reshape(3, -1)
+    f64 = l64[0].force.data.reshape(3, -1)
+    assert rel_l2(f32, f64) < 1e-6
+    assert np.abs(f64).max() > 0
+
+
+def test_f32_two_swimmer_arrays_accumulate():
+    from lbswim import swimmers
+    case = _spread_case()
+    lat, sw, tr, system = build_gpu(case, "f32")
+    s = case["swimmers"]
+    cp = swimmers.CommonParams()
+    for k in ("P", "l", "alpha", "mobility", "seed"):
+        setattr(cp, k, s[k])
+    sw2 = swimmers.Array(s["n"], cp)
+    sw2.r[:] = s["r"]
+    sw2.n[:] = s["nvec"]
+    sw2.v[:] = 0
+    sw2.H2D()
+    lat.ZeroForce()
+    sw.AddForces(lat)
+    sw2.AddForces(lat)
+    lat.force.D2H()
+    both = lat.force.data.reshape(3, -1).copy()
+    lat.ZeroForce()
+    sw.AddForces(lat)
+    lat.force.D2H()
+    one = lat.force.data.reshape(3, -1).copy()
+    assert rel_l2(both, 2 * one) < 1e-6
+    # a step taken with two pending arrays equals one taken from the dense field
+    system2 = build_gpu(case, "f32")
+    lat.ZeroForce()
+    sw.AddForces(lat)
+    sw2.AddForces(lat)
+    lat.Step()
+    lat.CalcHydro()
+    l2, s2a, _, _ = system2
+    s2b = swimmers.Array(s["n"], cp)
+    s2b.r[:] = s["r"]
+    s2b.n[:] = s["nvec"]
+    s2b.v[:] = 0
+    s2b.H2D()
+    l2.ZeroForce()
+    s2a.AddForces(l2)
+    s2b.AddForces(l2)
+    l2.force.D2H()
+    l2.Step()
+    l2.CalcHydro()
+    lat.u.D2H()
+    l2.u.D2H()
+    assert np.array_equal(lat.u.data, l2.u.data)
