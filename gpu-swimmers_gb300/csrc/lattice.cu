@@ -297,6 +297,12 @@ constexpr int FUSED_LX = 32;
 constexpr int FUSED_RING_THREADS = 96;
 constexpr int SPREAD_CAP = 256;  // ends of one slab held in shared memory
 
+// Local rows / columns of an end's four stencil nodes in a slab's cross-section.
+struct NodeLocal {
+  signed char y[4];
+  signed char z[4];
+};
+
 struct FusedArgs {
   const void* f_old;
   void* f_new;
@@ -327,7 +333,8 @@ template <int TZ, int TY, bool SPREAD>
 constexpr int fused_smem_bytes() {
   return RING_POP_PLANES * (TY + 2) * (TZ + 2) * (int)sizeof(float) +
          (SPREAD ? SPREAD_CAP * ((int)sizeof(EndRecord<float>) + 8) +
-                       2 * 3 * (TY + 2) * (TZ + 2) * (int)sizeof(long long)
+                       2 * 3 * (TY + 2) * (TZ + 2) * (int)sizeof(long long) +
+                       (FUSED_LX + 3) * 4 + SPREAD_CAP * (8 + FUSED_LX + 2)
                  : 0);
 }
 
@@ -378,6 +385,10 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   long long* fq = reinterpret_cast<long long*>(srec + SPREAD_CAP);  // [2][3][PLANE]
   // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 64
   unsigned long long* xmask = reinterpret_cast<unsigned long long*>(fq + 2 * 3 * PLANE);
+  // ends covering each local plane: plist[poff[kk] .. poff[kk + 1]) (indices into srec)
+  int* poff = reinterpret_cast<int*>(xmask + SPREAD_CAP);  // [FUSED_LX + 3]
+  NodeLocal* nodes = reinterpret_cast<NodeLocal*>(poff + FUSED_LX + 3);  // [SPREAD_CAP]
+  unsigned char* plist = reinterpret_cast<unsigned char*>(nodes + SPREAD_CAP);
   const float fx_scale = SPREAD ? a.fixed_scale[0] : 0.f;
   const float fx_inv = SPREAD ? a.fixed_scale[1] : 0.f;
   int cnt = 0;
@@ -396,11 +407,51 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
         for (int kk = 0; kk < ex + 2; ++kk)
           if (cover_weight(wrap_once(x0 - 1 + kk, nx), srec[q].o[0], nx, srec[q].phi[0], w))
             m |= 1ull << kk;
+        // local row / column of each stencil node in the halo-inclusive
+        // cross-section (-1: outside); bit 63 marks nodes that appear twice
+        NodeLocal nl;
+        for (int j = 0; j < 4; ++j) {
+          const int ly2 = wrap_any(wrap_any(srec[q].o[1] + j, ny) - y0 + 1, ny);
+          const int lz2 = wrap_any(wrap_any(srec[q].o[2] + j, nz) - z0 + 1, nz);
+          nl.y[j] = (signed char)(ly2 <= ey + 1 ? ly2 : -1);
+          nl.z[j] = (signed char)(lz2 <= ez + 1 ? lz2 : -1);
+          if (ly2 + ny <= ey + 1 || lz2 + nz <= ez + 1) m |= 1ull << 63;
+        }
+        nodes[q] = nl;
         xmask[q] = m;
       }
     }
     for (int i = tid; i < 2 * 3 * PLANE; i += blockDim.x) fq[i] = 0;
     __syncthreads();
+    if (in_smem) {
+      // per-plane lists in increasing end position: count, offsets, fill
+      const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+      for (int kk = warp; kk < ex + 2; kk += nwarps) {
+        int c = 0;
+        for (int base = 0; base < cnt; base += 32) {
+          const int q = base + lane;
+          c += __popc(__ballot_sync(0xffffffffu, q < cnt && ((xmask[q] >> kk) & 1ull)));
+        }
+        if (lane == 0) poff[kk + 1] = c;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        poff[0] = 0;
+        for (int kk = 0; kk < ex + 2; ++kk) poff[kk + 1] += poff[kk];
+      }
+      __syncthreads();
+      for (int kk = warp; kk < ex + 2; kk += nwarps) {
+        int at = poff[kk];
+        for (int base = 0; base < cnt; base += 32) {
+          const int q = base + lane;
+          const bool cov = q < cnt && ((xmask[q] >> kk) & 1ull);
+          const unsigned m = __ballot_sync(0xffffffffu, cov);
+          if (cov) plist[at + __popc(m & ((1u << lane) - 1u))] = (unsigned char)q;
+          at += __popc(m);
+        }
+      }
+      __syncthreads();
+    }
   }
   auto rec = [&](int q) -> const EndRecord<float>& {
     return in_smem ? srec[q] : a.ends[a.slab_list[s0 + q]];
@@ -410,26 +461,50 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   auto scatter_plane = [&](int kk, int buf) {
     const int gx = wrap_once(x0 - 1 + kk, nx);
     long long* f0 = fq + buf * 3 * PLANE;
-    for (int t = tid; t < cnt * 16; t += blockDim.x) {
-      if (in_smem && !((xmask[t >> 4] >> kk) & 1ull)) continue;
-      const EndRecord<float>& e = rec(t >> 4);
-      float wx;
-      if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
-      const int jy = (t >> 2) & 3, jz = t & 3;
-      const float py = e.phi[1][jy], pz = e.phi[2][jz];
-      const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-      const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-      const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
-      // every local copy of the node's site in the halo-inclusive cross-section
-      const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
-      for (int ly2 = wrap_any(yg - y0 + 1, ny); ly2 <= ey + 1; ly2 += ny)
-        for (int lz2 = wrap_any(zg - z0 + 1, nz); lz2 <= ez + 1; lz2 += nz) {
-          const int at = ly2 * HZ + lz2;
-          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + at), (unsigned long long)q0);
-          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + PLANE + at), (unsigned long long)q1);
-          atomicAdd(reinterpret_cast<unsigned long long*>(f0 + 2 * PLANE + at),
-                    (unsigned long long)q2);
+    auto add3 = [&](int at, long long q0, long long q1, long long q2) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + at), (unsigned long long)q0);
+      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + PLANE + at), (unsigned long long)q1);
+      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + 2 * PLANE + at), (unsigned long long)q2);
+    };
+    if (in_smem) {
+      // (end, node) pairs of the ends covering this plane, on contiguous threads
+      const int p0 = poff[kk], np = poff[kk + 1] - p0;
+      for (int t = tid; t < np * 16; t += blockDim.x) {
+        const int q = plist[p0 + (t >> 4)];
+        const EndRecord<float>& e = srec[q];
+        const int jy = (t >> 2) & 3, jz = t & 3;
+        const int ly2 = nodes[q].y[jy], lz2 = nodes[q].z[jz];
+        if ((ly2 | lz2) < 0) continue;  // node outside this cross-section
+        float wx;
+        cover_weight(gx, e.o[0], nx, e.phi[0], wx);
+        const float py = e.phi[1][jy], pz = e.phi[2][jz];
+        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+        if (!(xmask[q] >> 63)) {
+          add3(ly2 * HZ + lz2, q0, q1, q2);
+        } else {
+          // tiny lattice: a node can appear at several places of the cross-section
+          for (int a = ly2; a <= ey + 1; a += ny)
+            for (int b = lz2; b <= ez + 1; b += nz) add3(a * HZ + b, q0, q1, q2);
         }
+      }
+    } else {
+      // more ends than shared memory holds: every end, records from global memory
+      for (int t = tid; t < cnt * 16; t += blockDim.x) {
+        const EndRecord<float>& e = a.ends[a.slab_list[s0 + (t >> 4)]];
+        float wx;
+        if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
+        const int jy = (t >> 2) & 3, jz = t & 3;
+        const float py = e.phi[1][jy], pz = e.phi[2][jz];
+        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+        const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
+        for (int ly2 = wrap_any(yg - y0 + 1, ny); ly2 <= ey + 1; ly2 += ny)
+          for (int lz2 = wrap_any(zg - z0 + 1, nz); lz2 <= ez + 1; lz2 += nz)
+            add3(ly2 * HZ + lz2, q0, q1, q2);
+      }
     }
   };
   if (SPREAD) {

@@ -353,11 +353,22 @@ __device__ __forceinline__ float end_contrib_f(float wy, float wz, float wxF) {
 // force is the same whatever order the contributions arrive in: shared-memory
 // atomics in the step kernel and the gather of k_force_tile give identical
 // bits.  The host picks S so that the sum of all |c| stays below 2^62.
+// round(c * scale) as a 64-bit integer using only 32-bit conversions (the 64-bit
+// ones run on GB300's narrow FP64 pipe).  v = c * scale is exact (power of two);
+// when |v| >= 2^31 it is an integer with at most 24 significant bits, split
+// exactly into hi * 2^32 + lo.
 __device__ __forceinline__ long long fx_quant(float c, float scale) {
-  return __float2ll_rn(c * scale);
+  const float v = c * scale;
+  if (fabsf(v) < 2147483648.f) return (long long)__float2int_rn(v);
+  const float hi = floorf(v * 2.3283064365386963e-10f);  // v / 2^32
+  const float lo = v - hi * 4294967296.f;                 // exact, in [0, 2^32)
+  return (long long)(int)hi * 4294967296ll + (long long)__float2uint_rn(lo);
 }
+// float of the 64-bit sum q * inv_scale, from its two 32-bit halves.
 __device__ __forceinline__ float fx_value(long long q, float inv_scale) {
-  return __ll2float_rn(q) * inv_scale;
+  const int hi = (int)(q >> 32);
+  const unsigned lo = (unsigned)(q & 0xffffffffll);
+  return (__int2float_rn(hi) * 4294967296.f + __uint2float_rn(lo)) * inv_scale;
 }
 __device__ __forceinline__ float node_contrib(float py, float pz, float wx, float F) {
   return (py * pz) * (wx * F);

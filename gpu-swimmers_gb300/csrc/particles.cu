@@ -503,20 +503,39 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
 }
 
 // ---- Move kernels -----------------------------------------------------------
-// Stencil nodes and Peskin weights of position r (interp.cu:23-30).
+// Stencil nodes and Peskin weights of position r (interp.cu:23-30).  The FP64
+// path keeps the reference's arithmetic; the FP32 path takes one FP64
+// difference per axis and forms the four arguments in FP32 (GB300's FP64 pipe
+// is narrow).
 template <class T>
 __device__ __forceinline__ void interp_setup(const Dims& D, const double r[3], int idx[3][4],
                                              T phi[3][4]) {
   for (int d = 0; d < 3; ++d) {
     const double x0 = ceil(r[d] - 2.);
     const int o = wrap_any((int)x0, D.n[d]);
+    const float dr = (float)(r[d] - x0);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int t = o + i;
       while (t >= D.n[d]) t -= D.n[d];
       idx[d][i] = t;
-      phi[d][i] = peskin_delta<T>((T)(r[d] - (x0 + i)));
+      if constexpr (sizeof(T) == 8)
+        phi[d][i] = peskin_delta<T>(r[d] - (x0 + i));
+      else
+        phi[d][i] = peskin_delta<T>(dr - (float)i);
     }
+  }
+}
+
+// New periodic coordinate: the reference's fmod(r + size, size) on the FP64
+// path (SwimmerArray.cu:167, TracerArray.cu:40), a compare-and-shift on the
+// FP32 path (valid while a step moves a particle less than one box length).
+template <class T>
+__device__ __forceinline__ double wrap_position(double r, int n) {
+  if constexpr (sizeof(T) == 8) {
+    return fmod(r + n, (double)n);
+  } else {
+    return r >= n ? r - n : (r < 0.0 ? r + n : r);
   }
 }
 
@@ -591,7 +610,7 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     if (!c.translational_advection_off) rDot += (double)v[d];
     rMinus[d] = r[d] - n0[d] * c.l;
     swv[nsw * d + i] = rDot;
-    swr[nsw * d + i] = fmod(r[d] + rDot + D.n[d], (double)D.n[d]);
+    swr[nsw * d + i] = wrap_position<T>(r[d] + rDot, D.n[d]);
   }
   const float rnd = rng_uniform(seed, (uint32_t)i, step);
   double nn[3];
@@ -621,7 +640,7 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
   for (int d = 0; d < 3; ++d) {
     const double vd = (double)vv[d];
     v[ntr * d + i] = vd;
-    r[ntr * d + i] = fmod(rr[d] + vd + D.n[d], (double)D.n[d]);
+    r[ntr * d + i] = wrap_position<T>(rr[d] + vd, D.n[d]);
     s[ntr * d + i] += vd;
   }
 }
@@ -645,6 +664,225 @@ __global__ void k_rng_draws(unsigned long long seed, int n, unsigned long long s
   double nn[3];
   rng_normal3(seed, (uint32_t)i, step, nn);
   for (int d = 0; d < 3; ++d) g[n * d + i] = nn[d];
+}
+
+// ---- FP32-path Move kernels ------------------------------------------------------
+// A block moves NP particles in three phases.  (1) One thread per particle forms
+// its stencil -- wrapped node offsets and Peskin weights -- in shared memory.
+// (2) Sixteen threads per particle gather the 4^3 nodes: lane (y node, z node)
+// of the group loads the four x nodes, and the sixteen partial sums are added
+// with a fixed shuffle tree, so the result does not depend on scheduling.
+// (3) One thread per particle updates it.  GB300's FP64 pipe is narrow, so the
+// FP64 work of phases 1 and 3 is issued once per 32 particles and the stencil
+// origin comes from the bits of the position with integer operations.
+
+// Stencil of one interpolation point: wrapped origin node and Peskin weights.
+struct Stencil {
+  int o[3];
+  int active;  // 0: not gathered
+  float wx[4], wy[4], wz[4];
+};
+
+// x0 = ceil(x - 2) and dr = (float)(x - x0) for one coordinate, with the
+// rounding of those FP64 operations.  For 0 <= x < 2^30 both come from the
+// bits of x by integer operations: x - x0 is exact in FP64 unless x < 1, where
+// 1 + x is first rounded to FP64's 52 fraction bits, then to FP32's 23.  Other
+// values take FP64.
+__device__ __forceinline__ void stencil_axis(double x, int& x0, float& dr) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)(b >> 52);  // biased exponent; negative x gives ex >= 2048
+  if (ex >= 1023 + 30) {
+    const double c = ceil(x - 2.);
+    x0 = (int)c;
+    dr = (float)(x - c);
+    return;
+  }
+  if (ex < 1023 - 40) {  // 0 <= x < 2^-40: x - 2 rounds to -2 when x <= 2^-53
+    const bool low = b <= (970ull << 52);
+    x0 = low ? -2 : -1;
+    dr = low ? 2.f : 1.f;
+    return;
+  }
+  const unsigned long long mant = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int shift = 1075 - ex;  // x = mant * 2^-shift, 23 <= shift <= 92
+  unsigned long long f52;       // fraction of x - x0 in 2^-52 units
+  if (shift <= 52) {
+    const unsigned long long fr = mant & ((1ull << shift) - 1);
+    const int cell = (int)(mant >> shift);
+    if (fr == 0) {  // x is an integer
+      x0 = cell - 2;
+      dr = 2.f;
+      return;
+    }
+    x0 = cell - 1;
+    f52 = fr << (52 - shift);
+  } else {  // 2^-40 <= x < 1
+    x0 = -1;
+    const int s = shift - 52;  // 1 .. 40
+    const unsigned long long rem = mant & ((1ull << s) - 1), half = 1ull << (s - 1);
+    f52 = mant >> s;
+    f52 += (rem > half || (rem == half && (f52 & 1ull))) ? 1ull : 0ull;
+  }
+  // to 23 fraction bits; a carry out gives 2.0f
+  unsigned m = (unsigned)(f52 >> 29);
+  const unsigned rem = (unsigned)(f52 & 0x1fffffffull);
+  m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  dr = __int_as_float(0x3f800000 + (int)m);
+}
+
+__device__ __forceinline__ void point_stencil(const Dims& D, const double r[3], Stencil& st) {
+  float dr[3];
+  for (int d = 0; d < 3; ++d) {
+    int x0;
+    stencil_axis(r[d], x0, dr[d]);
+    st.o[d] = wrap_any(x0, D.n[d]);
+  }
+  st.active = 1;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    st.wx[j] = peskin_delta<float>(dr[0] - (float)j);
+    st.wy[j] = peskin_delta<float>(dr[1] - (float)j);
+    st.wz[j] = peskin_delta<float>(dr[2] - (float)j);
+  }
+}
+
+__device__ __forceinline__ int node_after(int o, int j, int n) {
+  int t = o + j;
+  while (t >= n) t -= n;
+  return t;
+}
+
+__device__ __forceinline__ void reduce16(float& vx, float& vy, float& vz) {
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) {
+    vx += __shfl_xor_sync(0xffffffffu, vx, off);
+    vy += __shfl_xor_sync(0xffffffffu, vy, off);
+    vz += __shfl_xor_sync(0xffffffffu, vz, off);
+  }
+}
+
+__device__ __forceinline__ void gather_point(const float4* __restrict__ h, const Dims& D,
+                                             const Stencil& s, int jy, int kz, float& vx,
+                                             float& vy, float& vz) {
+  vx = vy = vz = 0.f;
+  if (!s.active) return;
+  const int nz = D.n[2], nynz = D.n[1] * D.n[2];
+  const int yz = node_after(s.o[1], jy, D.n[1]) * nz + node_after(s.o[2], kz, nz);
+  const float wyz = s.wy[jy] * s.wz[kz];
+#pragma unroll
+  for (int ix = 0; ix < 4; ++ix) {
+    const float4 q = __ldg(h + node_after(s.o[0], ix, D.n[0]) * nynz + yz);
+    const float w = s.wx[ix] * wyz;
+    vx += w * q.x;
+    vy += w * q.y;
+    vz += w * q.z;
+  }
+}
+
+// Phase 2: the block's threads, sixteen per point and two points per group at a
+// time, gather the velocity of npts stencils.  Every thread runs the same
+// number of iterations (npts is a multiple of blockDim / 8).
+__device__ __forceinline__ void gather_block(const float4* __restrict__ h, const Dims& D,
+                                             const Stencil* st, int npts, float3* vel) {
+  const int sub = threadIdx.x & 15, jy = sub >> 2, kz = sub & 3;
+  const int groups = blockDim.x >> 4;
+  for (int p = threadIdx.x >> 4; p < npts; p += 2 * groups) {
+    float ax, ay, az, bx, by, bz;
+    gather_point(h, D, st[p], jy, kz, ax, ay, az);
+    gather_point(h, D, st[p + groups], jy, kz, bx, by, bz);
+    reduce16(ax, ay, az);
+    reduce16(bx, by, bz);
+    if (sub == 0) {
+      vel[p] = make_float3(ax, ay, az);
+      vel[p + groups] = make_float3(bx, by, bz);
+    }
+  }
+}
+
+constexpr int TRACER_MOVE_BLOCK = 256;
+
+__global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
+    int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
+    const float4* __restrict__ h) {
+  __shared__ Stencil st[TRACER_MOVE_BLOCK];
+  __shared__ float3 vel[TRACER_MOVE_BLOCK];
+  const int i = blockIdx.x * TRACER_MOVE_BLOCK + threadIdx.x;
+  const bool valid = i < ntr;
+  double rr[3] = {0.0, 0.0, 0.0};
+  if (valid) {
+    for (int d = 0; d < 3; ++d) rr[d] = r[(long long)ntr * d + i];
+    point_stencil(D, rr, st[threadIdx.x]);
+  } else {
+    st[threadIdx.x].active = 0;
+  }
+  __syncthreads();
+  gather_block(h, D, st, TRACER_MOVE_BLOCK, vel);
+  __syncthreads();
+  if (!valid) return;
+  const float3 w = vel[threadIdx.x];
+  const float vv[3] = {w.x, w.y, w.z};
+  for (int d = 0; d < 3; ++d) {
+    const double vd = (double)vv[d];
+    v[(long long)ntr * d + i] = vd;
+    r[(long long)ntr * d + i] = wrap_position<float>(rr[d] + vd, D.n[d]);
+    s[(long long)ntr * d + i] += vd;
+  }
+}
+
+constexpr int SWIMMER_MOVE_BLOCK = 128;
+
+__global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
+    int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
+    lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
+    const float4* __restrict__ h) {
+  // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
+  __shared__ Stencil st[2 * SWIMMER_MOVE_BLOCK];
+  __shared__ float3 vel[2 * SWIMMER_MOVE_BLOCK];
+  const int t = threadIdx.x, i = blockIdx.x * SWIMMER_MOVE_BLOCK + t;
+  const bool valid = i < nsw;
+  double r[3] = {0.0, 0.0, 0.0}, n0[3] = {0.0, 0.0, 0.0};
+  bool tumble = false, rotate = false;
+  if (valid) {
+    for (int d = 0; d < 3; ++d) {
+      r[d] = swr[nsw * d + i];
+      n0[d] = swn[nsw * d + i];
+    }
+    tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
+    rotate = !tumble && !c.rotational_advection_off;
+    point_stencil(D, r, st[t]);
+    if (rotate) {
+      double rMinus[3];
+      for (int d = 0; d < 3; ++d) rMinus[d] = r[d] - n0[d] * c.l;
+      point_stencil(D, rMinus, st[SWIMMER_MOVE_BLOCK + t]);
+    } else {
+      st[SWIMMER_MOVE_BLOCK + t].active = 0;
+    }
+  } else {
+    st[t].active = 0;
+    st[SWIMMER_MOVE_BLOCK + t].active = 0;
+  }
+  __syncthreads();
+  gather_block(h, D, st, 2 * SWIMMER_MOVE_BLOCK, vel);
+  __syncthreads();
+  if (!valid) return;
+  const float3 w = vel[t], wm = vel[SWIMMER_MOVE_BLOCK + t];
+  const float v[3] = {w.x, w.y, w.z}, vm[3] = {wm.x, wm.y, wm.z};
+  for (int d = 0; d < 3; ++d) {
+    double rDot = c.mobility * c.P * n0[d];
+    if (!c.translational_advection_off) rDot += (double)v[d];
+    swv[nsw * d + i] = rDot;
+    swr[nsw * d + i] = wrap_position<float>(r[d] + rDot, D.n[d]);
+  }
+  double nn[3];
+  if (tumble) {
+    rng_normal3(seed, (uint32_t)i, step, nn);
+  } else if (rotate) {
+    for (int d = 0; d < 3; ++d) nn[d] = n0[d] + ((double)v[d] - (double)vm[d]) / c.l;
+  } else {
+    return;
+  }
+  const double norm = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+  for (int d = 0; d < 3; ++d) swn[nsw * d + i] = nn[d] / norm;
 }
 
 // ---- host side -----------------------------------------------------------------
@@ -867,8 +1105,12 @@ void swimmers_move(Swimmers* W, Lattice* L) {
     if (L->precision == LBSWIM_F64)
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u);
-    else
+    else if (L->n >= (1ll << 31))  // node offsets beyond int
       k_swimmers_move<float4, float><<<grid, 256, 0, L->stream>>>(
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
+    else
+      k_swimmers_move_f32<<<(W->n + SWIMMER_MOVE_BLOCK - 1) / SWIMMER_MOVE_BLOCK,
+                            SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     LB_CHECK_LAUNCH(1);
   }
@@ -1027,9 +1269,12 @@ void tracers_move(Tracers* T, Lattice* L) {
   if (L->precision == LBSWIM_F64)
     k_tracers_move<double, double><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
                                                                  (const double*)L->u);
-  else
+  else if (L->n >= (1ll << 31))  // node offsets beyond int
     k_tracers_move<float4, float><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
                                                                 L->hydro);
+  else
+    k_tracers_move_f32<<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK, TRACER_MOVE_BLOCK,
+                         0, L->stream>>>(T->n, T->r, T->s, T->v, D, L->hydro);
   LB_CHECK_LAUNCH(1);
 }
 
