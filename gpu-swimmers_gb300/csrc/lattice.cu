@@ -296,11 +296,19 @@ __global__ void k_f32_to_f64(const float* __restrict__ src, double* __restrict__
 constexpr int FUSED_LX = 32;
 constexpr int FUSED_RING_THREADS = 96;
 constexpr int SPREAD_CAP = 256;  // ends of one slab held in shared memory
+constexpr int SPREAD_PLANES_PER_END = 8;  // local planes one end can cover (6 at most)
 
 // Local rows / columns of an end's four stencil nodes in a slab's cross-section.
 struct NodeLocal {
   signed char y[4];
   signed char z[4];
+};
+
+// What the scatter needs of a pending dipole end, kept in shared memory.
+struct SlabEnd {
+  int ox;          // wrapped x origin of the stencil
+  float F[3];      // force carried by the end
+  float phi[3][4];  // Peskin weights of the 4 nodes per axis
 };
 
 struct FusedArgs {
@@ -322,30 +330,56 @@ struct FusedArgs {
 // Post-collision populations wait in shared memory until the output plane can
 // pull them: those moving +x (1, 7-10) are read two planes later, those at rest
 // in x (0, 3-6) one plane later, those moving -x (2, 11-14) in the same plane.
-// With one barrier per plane that needs 4, 3 and 2 slots of 5 populations.
+// With one barrier per plane that needs 4, 3 and 2 slots of 5 populations; the
+// SPREAD instances take a second barrier per plane and need 3, 2 and 1, which
+// leaves room in shared memory for the spreading without shrinking the L1
+// cache that holds the loads in flight.
 __host__ __device__ constexpr int ring_group(int p) { return cx_of(p) > 0 ? 0 : (cx_of(p) == 0 ? 1 : 2); }
 __host__ __device__ constexpr int ring_index(int p) {
   return p == 1 || p == 0 || p == 2 ? 0 : (p <= 6 ? p - 2 : (p <= 10 ? p - 6 : p - 10));
 }
-constexpr int RING_POP_PLANES = 5 * (4 + 3 + 2);
+template <bool SPREAD>
+__host__ __device__ constexpr int ring_slots(int group) {
+  return SPREAD ? 3 - group : 4 - group;
+}
+template <bool SPREAD>
+__host__ __device__ constexpr int ring_pop_planes() {
+  return 5 * (ring_slots<SPREAD>(0) + ring_slots<SPREAD>(1) + ring_slots<SPREAD>(2));
+}
+
+__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
+
+// Shared-memory layout of the SPREAD instances after the ring: fixed-point
+// force sums of one plane [3][PLANE] (int64), coverage masks [CAP] (u64), ends
+// [CAP], local node rows [CAP], per-plane list offsets [LX + 3], lists.
+template <int TZ, int TY>
+struct SpreadLayout {
+  static constexpr int PLANE = (TY + 2) * (TZ + 2);
+  static constexpr int ring = align16(ring_pop_planes<true>() * PLANE * 4);
+  static constexpr int fq = ring;
+  static constexpr int xmask = align16(fq + 3 * PLANE * 8);
+  static constexpr int ends = align16(xmask + SPREAD_CAP * 8);
+  static constexpr int nodes = align16(ends + SPREAD_CAP * (int)sizeof(SlabEnd));
+  static constexpr int poff = align16(nodes + SPREAD_CAP * (int)sizeof(NodeLocal));
+  static constexpr int plist = align16(poff + (FUSED_LX + 3) * 4);
+  static constexpr int total = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END);
+};
 
 template <int TZ, int TY, bool SPREAD>
 constexpr int fused_smem_bytes() {
-  return RING_POP_PLANES * (TY + 2) * (TZ + 2) * (int)sizeof(float) +
-         (SPREAD ? SPREAD_CAP * ((int)sizeof(EndRecord<float>) + 8) +
-                       2 * 3 * (TY + 2) * (TZ + 2) * (int)sizeof(long long) +
-                       (FUSED_LX + 3) * 4 + SPREAD_CAP * (8 + FUSED_LX + 2)
-                 : 0);
+  return SPREAD ? SpreadLayout<TZ, TY>::total
+                : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
 
 template <class S, int TZ, int TY, bool SPREAD>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
-  extern __shared__ __align__(16) float sm[];
-  float* ringA = sm;                     // [4][5][PLANE]
-  float* ringB = ringA + 4 * 5 * PLANE;  // [3][5][PLANE]
-  float* ringC = ringB + 3 * 5 * PLANE;  // [2][5][PLANE]
+  constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* ringA = reinterpret_cast<float*>(smraw);  // [NA][5][PLANE]
+  float* ringB = ringA + NA * 5 * PLANE;           // [NB][5][PLANE]
+  float* ringC = ringB + NB * 5 * PLANE;           // [NC][5][PLANE]
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * FUSED_LX;
@@ -380,15 +414,17 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   const float* __restrict__ F = a.force;
   const int my = ly * HZ + lz;
 
-  // ---- this slab's pending dipole ends and the fixed-point force planes ----
-  EndRecord<float>* srec = reinterpret_cast<EndRecord<float>*>(sm + RING_POP_PLANES * PLANE);
-  long long* fq = reinterpret_cast<long long*>(srec + SPREAD_CAP);  // [2][3][PLANE]
-  // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 64
-  unsigned long long* xmask = reinterpret_cast<unsigned long long*>(fq + 2 * 3 * PLANE);
+  // ---- this slab's pending dipole ends and the fixed-point force plane ----
+  using SL = SpreadLayout<TZ, TY>;
+  long long* fq = reinterpret_cast<long long*>(smraw + SL::fq);  // [3][PLANE]
+  // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 63;
+  // bit 63: a node of end q appears twice in the cross-section (tiny lattices)
+  unsigned long long* xmask = reinterpret_cast<unsigned long long*>(smraw + SL::xmask);
+  SlabEnd* srec = reinterpret_cast<SlabEnd*>(smraw + SL::ends);
+  NodeLocal* nodes = reinterpret_cast<NodeLocal*>(smraw + SL::nodes);
   // ends covering each local plane: plist[poff[kk] .. poff[kk + 1]) (indices into srec)
-  int* poff = reinterpret_cast<int*>(xmask + SPREAD_CAP);  // [FUSED_LX + 3]
-  NodeLocal* nodes = reinterpret_cast<NodeLocal*>(poff + FUSED_LX + 3);  // [SPREAD_CAP]
-  unsigned char* plist = reinterpret_cast<unsigned char*>(nodes + SPREAD_CAP);
+  int* poff = reinterpret_cast<int*>(smraw + SL::poff);
+  unsigned char* plist = smraw + SL::plist;
   const float fx_scale = SPREAD ? a.fixed_scale[0] : 0.f;
   const float fx_inv = SPREAD ? a.fixed_scale[1] : 0.f;
   int cnt = 0;
@@ -401,27 +437,33 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     in_smem = cnt <= SPREAD_CAP;
     if (in_smem) {
       for (int q = tid; q < cnt; q += blockDim.x) {
-        srec[q] = a.ends[a.slab_list[s0 + q]];
+        const EndRecord<float>& g = a.ends[a.slab_list[s0 + q]];
+        SlabEnd e;
+        e.ox = g.o[0];
+        for (int c = 0; c < 3; ++c) {
+          e.F[c] = g.F[c];
+          for (int j = 0; j < 4; ++j) e.phi[c][j] = g.phi[c][j];
+        }
         unsigned long long m = 0ull;
         float w;
         for (int kk = 0; kk < ex + 2; ++kk)
-          if (cover_weight(wrap_once(x0 - 1 + kk, nx), srec[q].o[0], nx, srec[q].phi[0], w))
-            m |= 1ull << kk;
+          if (cover_weight(wrap_once(x0 - 1 + kk, nx), e.ox, nx, e.phi[0], w)) m |= 1ull << kk;
         // local row / column of each stencil node in the halo-inclusive
-        // cross-section (-1: outside); bit 63 marks nodes that appear twice
+        // cross-section (-1: outside)
         NodeLocal nl;
         for (int j = 0; j < 4; ++j) {
-          const int ly2 = wrap_any(wrap_any(srec[q].o[1] + j, ny) - y0 + 1, ny);
-          const int lz2 = wrap_any(wrap_any(srec[q].o[2] + j, nz) - z0 + 1, nz);
+          const int ly2 = wrap_any(wrap_any(g.o[1] + j, ny) - y0 + 1, ny);
+          const int lz2 = wrap_any(wrap_any(g.o[2] + j, nz) - z0 + 1, nz);
           nl.y[j] = (signed char)(ly2 <= ey + 1 ? ly2 : -1);
           nl.z[j] = (signed char)(lz2 <= ez + 1 ? lz2 : -1);
           if (ly2 + ny <= ey + 1 || lz2 + nz <= ez + 1) m |= 1ull << 63;
         }
+        srec[q] = e;
         nodes[q] = nl;
         xmask[q] = m;
       }
     }
-    for (int i = tid; i < 2 * 3 * PLANE; i += blockDim.x) fq[i] = 0;
+    for (int i = tid; i < 3 * PLANE; i += blockDim.x) fq[i] = 0;
     __syncthreads();
     if (in_smem) {
       // per-plane lists in increasing end position: count, offsets, fill
@@ -453,30 +495,26 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
       __syncthreads();
     }
   }
-  auto rec = [&](int q) -> const EndRecord<float>& {
-    return in_smem ? srec[q] : a.ends[a.slab_list[s0 + q]];
-  };
-  // Add every end-node contribution of local plane kk into fq[buf]: the pairs
+  // Add every end-node contribution of local plane kk into fq: the pairs
   // (end, (jy, jz) node) are shared among all threads of the CTA.
-  auto scatter_plane = [&](int kk, int buf) {
+  auto scatter_plane = [&](int kk) {
     const int gx = wrap_once(x0 - 1 + kk, nx);
-    long long* f0 = fq + buf * 3 * PLANE;
     auto add3 = [&](int at, long long q0, long long q1, long long q2) {
-      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + at), (unsigned long long)q0);
-      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + PLANE + at), (unsigned long long)q1);
-      atomicAdd(reinterpret_cast<unsigned long long*>(f0 + 2 * PLANE + at), (unsigned long long)q2);
+      atomicAdd(reinterpret_cast<unsigned long long*>(fq + at), (unsigned long long)q0);
+      atomicAdd(reinterpret_cast<unsigned long long*>(fq + PLANE + at), (unsigned long long)q1);
+      atomicAdd(reinterpret_cast<unsigned long long*>(fq + 2 * PLANE + at), (unsigned long long)q2);
     };
     if (in_smem) {
       // (end, node) pairs of the ends covering this plane, on contiguous threads
       const int p0 = poff[kk], np = poff[kk + 1] - p0;
       for (int t = tid; t < np * 16; t += blockDim.x) {
         const int q = plist[p0 + (t >> 4)];
-        const EndRecord<float>& e = srec[q];
+        const SlabEnd& e = srec[q];
         const int jy = (t >> 2) & 3, jz = t & 3;
         const int ly2 = nodes[q].y[jy], lz2 = nodes[q].z[jz];
         if ((ly2 | lz2) < 0) continue;  // node outside this cross-section
         float wx;
-        cover_weight(gx, e.o[0], nx, e.phi[0], wx);
+        cover_weight(gx, e.ox, nx, e.phi[0], wx);
         const float py = e.phi[1][jy], pz = e.phi[2][jz];
         const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
         const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
@@ -485,8 +523,8 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
           add3(ly2 * HZ + lz2, q0, q1, q2);
         } else {
           // tiny lattice: a node can appear at several places of the cross-section
-          for (int a = ly2; a <= ey + 1; a += ny)
-            for (int b = lz2; b <= ez + 1; b += nz) add3(a * HZ + b, q0, q1, q2);
+          for (int a2 = ly2; a2 <= ey + 1; a2 += ny)
+            for (int b2 = lz2; b2 <= ez + 1; b2 += nz) add3(a2 * HZ + b2, q0, q1, q2);
         }
       }
     } else {
@@ -508,7 +546,7 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     }
   };
   if (SPREAD) {
-    scatter_plane(0, 0);
+    scatter_plane(0);
     __syncthreads();
   }
 
@@ -536,33 +574,41 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
     if (SPREAD && active) {
       // force = base + spread (k_force_tile writes the same bits)
-      long long* f0 = fq + (k & 1) * 3 * PLANE + my;
+      long long* f0 = fq + my;
       cur[15] += fx_value(f0[0], fx_inv);
       cur[16] += fx_value(f0[PLANE], fx_inv);
       cur[17] += fx_value(f0[2 * PLANE], fx_inv);
-      f0[0] = f0[PLANE] = f0[2 * PLANE] = 0;  // ready for plane k + 2
+      f0[0] = f0[PLANE] = f0[2 * PLANE] = 0;  // ready for plane k + 1
     }
+    // ring slots: plane k is written to A[k % NA], B[k % NB], C[k % NC]
+    const int wa_slot = SPREAD ? k3 : (k & 3);
+    const int wb_slot = SPREAD ? (k & 1) : k3;
+    const int wc_slot = SPREAD ? 0 : (k & 1);
     if (active) {
       float d[15];
 #pragma unroll
       for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>(cur[p], p);
       collide(d, cur[15], cur[16], cur[17], a.rho0, a.k, d);
-      float* wa = ringA + (k & 3) * 5 * PLANE + my;
-      float* wb = ringB + k3 * 5 * PLANE + my;
-      float* wc = ringC + (k & 1) * 5 * PLANE + my;
+      float* wa = ringA + wa_slot * 5 * PLANE + my;
+      float* wb = ringB + wb_slot * 5 * PLANE + my;
+      float* wc = ringC + wc_slot * 5 * PLANE + my;
 #pragma unroll
       for (int p = 0; p < 15; ++p) {
         float* w = ring_group(p) == 0 ? wa : (ring_group(p) == 1 ? wb : wc);
         w[ring_index(p) * PLANE] = d[p];
       }
     }
-    if (SPREAD && k + 1 < ex + 2) scatter_plane(k + 1, (k + 1) & 1);
     __syncthreads();
+    if (SPREAD && k + 1 < ex + 2) scatter_plane(k + 1);
     if (k >= 2 && interior) {
+      // output plane x = x0 + k - 2 pulls A of plane x-1, B of x, C of x+1
+      const int ra_slot = SPREAD ? (k3 == 2 ? 0 : k3 + 1) : ((k - 2) & 3);
+      const int rb_slot = SPREAD ? ((k - 1) & 1) : (k3 == 0 ? 2 : k3 - 1);
+      const int rc_slot = SPREAD ? 0 : (k & 1);
       const long long s = (long long)(x0 + k - 2) * nynz + yz;
-      const float* ra = ringA + ((k - 2) & 3) * 5 * PLANE + my;  // plane x-1: c_x = +1
-      const float* rb = ringB + (k3 == 0 ? 2 : k3 - 1) * 5 * PLANE + my;  // plane x
-      const float* rc = ringC + (k & 1) * 5 * PLANE + my;  // plane x+1: c_x = -1
+      const float* ra = ringA + ra_slot * 5 * PLANE + my;  // plane x-1: c_x = +1
+      const float* rb = ringB + rb_slot * 5 * PLANE + my;  // plane x
+      const float* rc = ringC + rc_slot * 5 * PLANE + my;  // plane x+1: c_x = -1
       float g[15];
 #pragma unroll
       for (int p = 0; p < 15; ++p) {
@@ -579,6 +625,9 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
       a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
                                (jz + 0.5f * Fp2) * inv, rho);
     }
+    // the next plane's collision overwrites the slots just read, and the
+    // scatter must be complete before the owners read it
+    if (SPREAD) __syncthreads();
     Fp0 = cur[15];
     Fp1 = cur[16];
     Fp2 = cur[17];

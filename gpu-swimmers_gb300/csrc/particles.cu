@@ -730,6 +730,101 @@ __device__ __forceinline__ void stencil_axis(double x, int& x0, float& dr) {
   dr = __int_as_float(0x3f800000 + (int)m);
 }
 
+// Exact FP64 value of a float, from its bits (no FP64 instruction).
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const int e = (int)((u >> 23) & 0xffu);
+  unsigned m = u & 0x7fffffu;
+  if (e == 255)  // inf / nan
+    return __longlong_as_double((long long)(sign | (0x7ffull << 52) | ((unsigned long long)m << 29)));
+  if (e == 0) {
+    if (m == 0) return __longlong_as_double((long long)sign);
+    const int msb = 31 - __clz((int)m);  // subnormal: m * 2^-149
+    const unsigned long long mant = ((unsigned long long)m << (52 - msb)) & 0xfffffffffffffull;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(msb - 149 + 1023) << 52) | mant));
+  }
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29)));
+}
+
+// Periodic coordinates as Q44 fixed point (44 fraction bits), for lattices
+// shorter than 2^19 sites per axis.  pos_to_q44 takes 0 <= r < 2^19 (else
+// returns false), rounding to nearest; q44_to_pos returns the FP64 nearest to
+// q * 2^-44, q >= 0.  Integer operations only.
+constexpr int Q44 = 44;
+__device__ __forceinline__ bool pos_to_q44(double r, long long& q) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+  const int ex = (int)(b >> 52);  // negative r gives ex >= 2048
+  if (ex >= 1023 + 19) return false;
+  if (ex < 1023 - Q44 - 2) {  // r < 2^-46 rounds to 0
+    q = 0;
+    return true;
+  }
+  const unsigned long long mant = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int sh = 1075 - Q44 - ex;  // q = mant * 2^-sh, -10 <= sh <= 55
+  if (sh <= 0) {
+    q = (long long)(mant << (-sh));
+  } else {
+    const unsigned long long rem = mant & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    unsigned long long v = mant >> sh;
+    v += (rem > half || (rem == half && (v & 1ull))) ? 1ull : 0ull;
+    q = (long long)v;
+  }
+  return true;
+}
+__device__ __forceinline__ double q44_to_pos(long long q) {
+  if (q <= 0) return 0.0;
+  const unsigned long long u = (unsigned long long)q;
+  const int msb = 63 - __clzll((long long)u);
+  int e = msb - Q44;
+  unsigned long long m;
+  if (msb <= 52) {
+    m = u << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    m = u >> sh;
+    m += (rem > half || (rem == half && (m & 1ull))) ? 1ull : 0ull;
+    if (m >> 53) {
+      m >>= 1;
+      ++e;
+    }
+  }
+  return __longlong_as_double(
+      (long long)(((unsigned long long)(e + 1023) << 52) | (m & 0xfffffffffffffull)));
+}
+
+// r + v moved back into [0, n) by one shift, like wrap_position<float>: in Q44
+// when r and r + v allow it, else in FP64.
+__device__ __forceinline__ double advance_position(double r, float v, int n) {
+  long long q;
+  if (n < (1 << 19) && fabsf(v) < (float)n && pos_to_q44(r, q)) {
+    q += fx_quant(v, 0x1.0p44f);
+    const long long nq = (long long)n << Q44;
+    q = q >= nq ? q - nq : (q < 0 ? q + nq : q);
+    return q44_to_pos(q);
+  }
+  return wrap_position<float>(r + f2d_exact(v), n);
+}
+
+// Three normal deviates of a tumble in FP32 from the counter blocks of
+// rng_normal3 (Box-Muller on 24-bit uniforms in (0, 1]).
+__device__ __forceinline__ void rng_normal3_f(uint64_t seed, uint32_t swimmer, uint64_t step,
+                                              float g[3]) {
+  uint32_t a[4], b[4];
+  rng_block(seed, swimmer, step, 1u, a);
+  rng_block(seed, swimmer, step, 2u, b);
+  const float r1 = sqrtf(-2.f * logf((float)((a[0] >> 8) + 1u) * 0x1.0p-24f));
+  const float r2 = sqrtf(-2.f * logf((float)((b[0] >> 8) + 1u) * 0x1.0p-24f));
+  float s1, c1, s2, c2;
+  sincospif((float)((a[2] >> 8) + 1u) * 0x1.0p-23f, &s1, &c1);
+  sincospif((float)((b[2] >> 8) + 1u) * 0x1.0p-23f, &s2, &c2);
+  g[0] = r1 * c1;
+  g[1] = r1 * s1;
+  g[2] = r2 * c2;
+}
+
 __device__ __forceinline__ void point_stencil(const Dims& D, const double r[3], Stencil& st) {
   float dr[3];
   for (int d = 0; d < 3; ++d) {
@@ -822,67 +917,75 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
   const float3 w = vel[threadIdx.x];
   const float vv[3] = {w.x, w.y, w.z};
   for (int d = 0; d < 3; ++d) {
-    const double vd = (double)vv[d];
+    const double vd = f2d_exact(vv[d]);
     v[(long long)ntr * d + i] = vd;
-    r[(long long)ntr * d + i] = wrap_position<float>(rr[d] + vd, D.n[d]);
+    r[(long long)ntr * d + i] = advance_position(rr[d], vv[d], D.n[d]);
     s[(long long)ntr * d + i] += vd;
   }
 }
 
-constexpr int SWIMMER_MOVE_BLOCK = 128;
+// Swimmers are few, so a block takes 16 of them on 256 threads: two stencils
+// (front and rear point) per swimmer, 16 threads per stencil.
+constexpr int SWIMMER_MOVE_BLOCK = 256;
+constexpr int SWIMMERS_PER_BLOCK = 16;
 
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
     lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
     const float4* __restrict__ h) {
+  constexpr int B = SWIMMERS_PER_BLOCK;
   // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
-  __shared__ Stencil st[2 * SWIMMER_MOVE_BLOCK];
-  __shared__ float3 vel[2 * SWIMMER_MOVE_BLOCK];
-  const int t = threadIdx.x, i = blockIdx.x * SWIMMER_MOVE_BLOCK + t;
-  const bool valid = i < nsw;
-  double r[3] = {0.0, 0.0, 0.0}, n0[3] = {0.0, 0.0, 0.0};
+  __shared__ Stencil st[2 * B];
+  __shared__ float3 vel[2 * B];
+  const int t = threadIdx.x, i = blockIdx.x * B + t;
+  const bool mine = t < B, valid = mine && i < nsw;
+  double r[3] = {0.0, 0.0, 0.0};
+  float n0[3] = {0.f, 0.f, 0.f};
   bool tumble = false, rotate = false;
   if (valid) {
+    double nd[3], rMinus[3];
     for (int d = 0; d < 3; ++d) {
       r[d] = swr[nsw * d + i];
-      n0[d] = swn[nsw * d + i];
+      nd[d] = swn[nsw * d + i];
+      n0[d] = (float)nd[d];
     }
     tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
     rotate = !tumble && !c.rotational_advection_off;
     point_stencil(D, r, st[t]);
     if (rotate) {
-      double rMinus[3];
-      for (int d = 0; d < 3; ++d) rMinus[d] = r[d] - n0[d] * c.l;
-      point_stencil(D, rMinus, st[SWIMMER_MOVE_BLOCK + t]);
+      for (int d = 0; d < 3; ++d) rMinus[d] = r[d] - nd[d] * c.l;
+      point_stencil(D, rMinus, st[B + t]);
     } else {
-      st[SWIMMER_MOVE_BLOCK + t].active = 0;
+      st[B + t].active = 0;
     }
-  } else {
+  } else if (mine) {
     st[t].active = 0;
-    st[SWIMMER_MOVE_BLOCK + t].active = 0;
+    st[B + t].active = 0;
   }
   __syncthreads();
-  gather_block(h, D, st, 2 * SWIMMER_MOVE_BLOCK, vel);
+  gather_block(h, D, st, 2 * B, vel);
   __syncthreads();
   if (!valid) return;
-  const float3 w = vel[t], wm = vel[SWIMMER_MOVE_BLOCK + t];
+  const float3 w = vel[t], wm = vel[B + t];
   const float v[3] = {w.x, w.y, w.z}, vm[3] = {wm.x, wm.y, wm.z};
+  const float mP = (float)(c.mobility * c.P);
   for (int d = 0; d < 3; ++d) {
-    double rDot = c.mobility * c.P * n0[d];
-    if (!c.translational_advection_off) rDot += (double)v[d];
-    swv[nsw * d + i] = rDot;
-    swr[nsw * d + i] = wrap_position<float>(r[d] + rDot, D.n[d]);
+    float rDot = mP * n0[d];
+    if (!c.translational_advection_off) rDot += v[d];
+    swv[nsw * d + i] = f2d_exact(rDot);
+    swr[nsw * d + i] = advance_position(r[d], rDot, D.n[d]);
   }
-  double nn[3];
+  float nn[3];
   if (tumble) {
-    rng_normal3(seed, (uint32_t)i, step, nn);
+    rng_normal3_f(seed, (uint32_t)i, step, nn);
   } else if (rotate) {
-    for (int d = 0; d < 3; ++d) nn[d] = n0[d] + ((double)v[d] - (double)vm[d]) / c.l;
+    const float inv_l = 1.f / (float)c.l;
+    for (int d = 0; d < 3; ++d) nn[d] = n0[d] + (v[d] - vm[d]) * inv_l;
   } else {
     return;
   }
-  const double norm = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
-  for (int d = 0; d < 3; ++d) swn[nsw * d + i] = nn[d] / norm;
+  const float inv = 1.f / sqrtf(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+  for (int d = 0; d < 3; ++d) swn[nsw * d + i] = f2d_exact(nn[d] * inv);
 }
 
 // ---- host side -----------------------------------------------------------------
@@ -1109,7 +1212,7 @@ void swimmers_move(Swimmers* W, Lattice* L) {
       k_swimmers_move<float4, float><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     else
-      k_swimmers_move_f32<<<(W->n + SWIMMER_MOVE_BLOCK - 1) / SWIMMER_MOVE_BLOCK,
+      k_swimmers_move_f32<<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
                             SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     LB_CHECK_LAUNCH(1);
