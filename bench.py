@@ -303,6 +303,7 @@ def our_arm(args, world, rank, local):
     ev0.record(stream)
     for _ in range(args.steps):
         system.Step()
+    lat.join()  # the last tracer moves run on the tracers' stream
     ev1.record(stream)
     barrier()
     launches = _lib.kernel_launches() - launches0

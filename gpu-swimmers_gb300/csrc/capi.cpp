@@ -92,6 +92,7 @@ int lbswim_lattice_destroy(lbswim_lattice* lat) {
   API_BEGIN
   if (!lat) return LBSWIM_OK;
   Lattice* L = reinterpret_cast<Lattice*>(lat);
+  lattice_join(L);
   cudaStreamSynchronize(L->stream);
   lattice_free(L);
   delete L;
@@ -118,6 +119,7 @@ int lbswim_lattice_calc_hydro(lbswim_lattice* lat) {
 int lbswim_lattice_init_from_hydro(lbswim_lattice* lat) {
   API_BEGIN
   check_lattice(lat);
+  lattice_join(LAT(lat));
   lattice_init_from_hydro(LAT(lat));
   API_END
 }
@@ -136,6 +138,7 @@ int lbswim_lattice_h2d(lbswim_lattice* lat, int field, const double* host) {
   check_lattice(lat);
   REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
   REQUIRE(host, "host buffer is NULL");
+  lattice_join(LAT(lat));
   lattice_h2d(LAT(lat), field, host);
   API_END
 }
@@ -145,6 +148,7 @@ int lbswim_lattice_d2h(lbswim_lattice* lat, int field, double* host) {
   check_lattice(lat);
   REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
   REQUIRE(host, "host buffer is NULL");
+  lattice_join(LAT(lat));
   lattice_d2h(LAT(lat), field, host);
   API_END
 }
@@ -206,6 +210,7 @@ int lbswim_lattice_set_stream(lbswim_lattice* lat, void* stream) {
   API_BEGIN
   check_lattice(lat);
   Lattice* L = LAT(lat);
+  lattice_join(L);
   LB_CUDA(cudaStreamSynchronize(L->stream));
   L->stream = (cudaStream_t)stream;
   API_END
@@ -214,7 +219,15 @@ int lbswim_lattice_set_stream(lbswim_lattice* lat, void* stream) {
 int lbswim_lattice_synchronize(lbswim_lattice* lat) {
   API_BEGIN
   check_lattice(lat);
+  lattice_join(LAT(lat));
   LB_CUDA(cudaStreamSynchronize(LAT(lat)->stream));
+  API_END
+}
+
+int lbswim_lattice_join(lbswim_lattice* lat) {
+  API_BEGIN
+  check_lattice(lat);
+  lattice_join(LAT(lat));
   API_END
 }
 
@@ -224,7 +237,9 @@ int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, 
   REQUIRE(ptr, "ptr is NULL");
   REQUIRE(field >= LBSWIM_FIELD_RHO && field <= LBSWIM_FIELD_FNEW, "unknown lattice field");
   Lattice* L = const_cast<Lattice*>(CLAT(lat));
+  lattice_join(L);
   if (field == LBSWIM_FIELD_FORCE) lattice_materialise_force(L);
+  LB_CUDA(cudaStreamSynchronize(L->stream));
   const bool packed = L->precision != LBSWIM_F64;
   switch (field) {
     case LBSWIM_FIELD_RHO: *ptr = packed ? (void*)L->hydro : L->rho; break;
@@ -496,8 +511,16 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
     for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
     lattice_step(L);
     lattice_calc_hydro(L);
+    // Tracers move on their own streams while the swimmers move and the next
+    // step spreads forces; the step after that waits before overwriting the
+    // velocities they read.
+    if (n_tracers > 0) {
+      if (!L->hydro_ready)
+        LB_CUDA(cudaEventCreateWithFlags(&L->hydro_ready, cudaEventDisableTiming));
+      LB_CUDA(cudaEventRecord(L->hydro_ready, L->stream));
+      for (int i = 0; i < n_tracers; ++i) tracers_move_async(TR(tracers[i]), L);
+    }
     for (int i = 0; i < n_swimmers; ++i) swimmers_move(SW(swimmers[i]), L);
-    for (int i = 0; i < n_tracers; ++i) tracers_move(TR(tracers[i]), L);
   }
   API_END
 }

@@ -678,6 +678,9 @@ void lattice_free(Lattice* L) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   spread_free(L->spread);
+  for (auto& r : L->readers) cudaEventDestroy(r.second);
+  for (cudaEvent_t e : L->reader_pool) cudaEventDestroy(e);
+  if (L->hydro_ready) cudaEventDestroy(L->hydro_ready);
   for (auto& p : L->timed) {
     cudaEventDestroy(p.first);
     cudaEventDestroy(p.second);
@@ -813,8 +816,22 @@ void lattice_read_timing(Lattice* L, double* total_ms, int* launches) {
   L->timed.clear();
 }
 
+void lattice_wait_readers(Lattice* L, const void* buf) {
+  for (size_t i = 0; i < L->readers.size();) {
+    if (buf == nullptr || L->readers[i].first == buf) {
+      LB_CUDA(cudaStreamWaitEvent(L->stream, L->readers[i].second, 0));
+      L->reader_pool.push_back(L->readers[i].second);
+      L->readers.erase(L->readers.begin() + i);
+    } else {
+      ++i;
+    }
+  }
+}
+
 void lattice_step(Lattice* L) {
   const int nx = L->size[0], ny = L->size[1], nz = L->size[2];
+  // the step writes rho, u into the shadow buffer of reduced-precision lattices
+  if (L->precision != LBSWIM_F64) lattice_wait_readers(L, L->hydro_shadow);
   std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
   if (L->timing) {
     ev = timing_pair(L);
@@ -871,6 +888,7 @@ void lattice_calc_hydro(Lattice* L) {
     return;
   }
   lattice_materialise_force(L);
+  lattice_wait_readers(L, L->precision == LBSWIM_F64 ? nullptr : (const void*)L->hydro);
   switch (L->precision) {
     case LBSWIM_F64: calc_hydro_t<double>(L); break;
     case LBSWIM_F32: calc_hydro_t<float>(L); break;

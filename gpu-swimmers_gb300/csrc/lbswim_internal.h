@@ -106,6 +106,11 @@ struct Lattice {
   double* staging = nullptr;  // FP64 staging for conversions
   size_t staging_elems = 0;
   int fused_tile = 0;  // 0 = 32x8 cross-section, 1 = 16x16
+  // Kernels on other streams that still read a velocity buffer: (buffer, event
+  // recorded after them).  Work that writes the buffer waits for the events.
+  std::vector<std::pair<const void*, cudaEvent_t>> readers;
+  std::vector<cudaEvent_t> reader_pool;
+  cudaEvent_t hydro_ready = nullptr;  // recorded on stream after CalcHydro
   // CUDA-event timing of the LB step kernel (lbswim_lattice_set_timing)
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;  // recorded, not yet read
@@ -146,6 +151,11 @@ struct Tracers {
   unsigned* bin_count = nullptr;
   unsigned* bin_start = nullptr;
   unsigned* scan_tmp = nullptr;
+  // System steps move tracers on their own stream, concurrently with the
+  // swimmers and the next force spreading; `done` follows the last such move.
+  cudaStream_t side = nullptr;
+  cudaEvent_t done = nullptr;
+  bool side_pending = false;
 };
 
 // lattice.cu
@@ -161,6 +171,10 @@ void lattice_d2h(Lattice* L, int field, double* host);
 void fill_params(lbswim_lbparams* p, double tau_s, double tau_b);
 void lattice_read_timing(Lattice* L, double* total_ms, int* launches);
 void lattice_zero_force(Lattice* L);
+// Make the lattice stream wait for the other-stream readers of `buf` (all
+// readers when buf is null).
+void lattice_wait_readers(Lattice* L, const void* buf);
+inline void lattice_join(Lattice* L) { lattice_wait_readers(L, nullptr); }
 
 // particles.cu: force spreading state
 void spread_materialise(Lattice* L);
@@ -171,6 +185,9 @@ void spread_free(SpreadScratch& S);
 void swimmers_add_forces(Swimmers* S, Lattice* L);
 void swimmers_move(Swimmers* S, Lattice* L);
 void tracers_move(Tracers* T, Lattice* L);
+// Move on the tracers' own stream after the point of the lattice stream where
+// L->hydro_ready was last recorded.
+void tracers_move_async(Tracers* T, Lattice* L);
 void tracers_alloc(Tracers* T);
 void tracers_free(Tracers* T);
 void tracers_h2d(Tracers* T, int field, const double* host);

@@ -1288,6 +1288,12 @@ void tracers_alloc(Tracers* T) {
 }
 
 void tracers_free(Tracers* T) {
+  if (T->side) {
+    cudaStreamSynchronize(T->side);
+    cudaStreamDestroy(T->side);
+    cudaEventDestroy(T->done);
+    T->side = nullptr;
+  }
   void* ptrs[] = {T->r,    T->s,      T->v,      T->r2,        T->s2,        T->v2,
                   T->perm, T->perm2,  T->bin_of, T->staging,   T->bin_count, T->bin_start,
                   T->scan_tmp};
@@ -1327,13 +1333,13 @@ void tracers_d2h(Tracers* T, int field, double* host) {
   }
 }
 
-static void tracers_sort(Tracers* T, Lattice* L) {
+static void tracers_sort(Tracers* T, Lattice* L, cudaStream_t stream) {
   const Dims D = make_dims(L);
   const int nb0 = (D.n[0] + TR_BIN - 1) / TR_BIN, nb1 = (D.n[1] + TR_BIN - 1) / TR_BIN,
             nb2 = (D.n[2] + TR_BIN - 1) / TR_BIN;
   const int nbins = nb0 * nb1 * nb2;
   if (T->nbins != nbins) {
-    LB_CUDA(cudaStreamSynchronize(L->stream));
+    LB_CUDA(cudaStreamSynchronize(stream));
     if (T->bin_count) cudaFree(T->bin_count);
     if (T->bin_start) cudaFree(T->bin_start);
     if (T->scan_tmp) cudaFree(T->scan_tmp);
@@ -1341,17 +1347,17 @@ static void tracers_sort(Tracers* T, Lattice* L) {
     LB_CUDA(cudaMalloc(&T->bin_count, sizeof(unsigned) * nbins));
     LB_CUDA(cudaMalloc(&T->bin_start, sizeof(unsigned) * (nbins + 1)));
     LB_CUDA(cudaMalloc(&T->scan_tmp, sizeof(unsigned) * ((nbins + SCAN_TILE - 1) / SCAN_TILE)));
-    LB_CUDA(cudaMemsetAsync(T->bin_count, 0, sizeof(unsigned) * nbins, L->stream));
+    LB_CUDA(cudaMemsetAsync(T->bin_count, 0, sizeof(unsigned) * nbins, stream));
     T->nbins = nbins;
   }
   const int g = (T->n + 255) / 256;
-  k_tr_bin<<<g, 256, 0, L->stream>>>(T->n, T->r, D, nb1, nb2, T->bin_of, T->bin_count);
+  k_tr_bin<<<g, 256, 0, stream>>>(T->n, T->r, D, nb1, nb2, T->bin_of, T->bin_count);
   const int nscan = (nbins + SCAN_TILE - 1) / SCAN_TILE;
-  k_scan_tiles<<<nscan, SCAN_THREADS, 0, L->stream>>>(T->bin_count, nbins, T->scan_tmp);
-  k_scan_top<<<1, 1024, 0, L->stream>>>(T->scan_tmp, nscan);
-  k_scan_apply<<<nscan, SCAN_THREADS, 0, L->stream>>>(T->bin_count, nbins, T->scan_tmp,
+  k_scan_tiles<<<nscan, SCAN_THREADS, 0, stream>>>(T->bin_count, nbins, T->scan_tmp);
+  k_scan_top<<<1, 1024, 0, stream>>>(T->scan_tmp, nscan);
+  k_scan_apply<<<nscan, SCAN_THREADS, 0, stream>>>(T->bin_count, nbins, T->scan_tmp,
                                                       T->bin_start, (unsigned)T->n);
-  k_tr_permute<<<g, 256, 0, L->stream>>>(T->n, T->bin_of, T->bin_count, T->bin_start, T->r,
+  k_tr_permute<<<g, 256, 0, stream>>>(T->n, T->bin_of, T->bin_count, T->bin_start, T->r,
                                          T->s, T->v, T->perm, T->r2, T->s2, T->v2, T->perm2);
   LB_CHECK_LAUNCH(5);
   std::swap(T->r, T->r2);
@@ -1363,22 +1369,48 @@ static void tracers_sort(Tracers* T, Lattice* L) {
   T->moves_since_sort = 0;
 }
 
-void tracers_move(Tracers* T, Lattice* L) {
-  if (T->n <= 0) return;
-  if (T->needs_sort || T->moves_since_sort >= TRACER_RESORT_MOVES) tracers_sort(T, L);
+static void tracers_move_on(Tracers* T, Lattice* L, cudaStream_t stream) {
+  if (T->needs_sort || T->moves_since_sort >= TRACER_RESORT_MOVES) tracers_sort(T, L, stream);
   T->moves_since_sort++;
   const Dims D = make_dims(L);
   const int grid = (T->n + 255) / 256;
   if (L->precision == LBSWIM_F64)
-    k_tracers_move<double, double><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
+    k_tracers_move<double, double><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
                                                                  (const double*)L->u);
   else if (L->n >= (1ll << 31))  // node offsets beyond int
-    k_tracers_move<float4, float><<<grid, 256, 0, L->stream>>>(T->n, T->r, T->s, T->v, D,
+    k_tracers_move<float4, float><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
                                                                 L->hydro);
   else
     k_tracers_move_f32<<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK, TRACER_MOVE_BLOCK,
-                         0, L->stream>>>(T->n, T->r, T->s, T->v, D, L->hydro);
+                         0, stream>>>(T->n, T->r, T->s, T->v, D, L->hydro);
   LB_CHECK_LAUNCH(1);
+}
+
+void tracers_move(Tracers* T, Lattice* L) {
+  if (T->n <= 0) return;
+  if (T->side_pending) LB_CUDA(cudaStreamWaitEvent(L->stream, T->done, 0));
+  tracers_move_on(T, L, L->stream);
+}
+
+void tracers_move_async(Tracers* T, Lattice* L) {
+  if (T->n <= 0) return;
+  if (!T->side) {
+    LB_CUDA(cudaStreamCreateWithFlags(&T->side, cudaStreamNonBlocking));
+    LB_CUDA(cudaEventCreateWithFlags(&T->done, cudaEventDisableTiming));
+  }
+  LB_CUDA(cudaStreamWaitEvent(T->side, L->hydro_ready, 0));
+  tracers_move_on(T, L, T->side);
+  LB_CUDA(cudaEventRecord(T->done, T->side));
+  T->side_pending = true;
+  cudaEvent_t ev;
+  if (L->reader_pool.empty()) {
+    LB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } else {
+    ev = L->reader_pool.back();
+    L->reader_pool.pop_back();
+  }
+  LB_CUDA(cudaEventRecord(ev, T->side));
+  L->readers.emplace_back(L->precision == LBSWIM_F64 ? (const void*)L->u : (const void*)L->hydro, ev);
 }
 
 void lattice_interp_velocity(Lattice* L, int np, const double* r_host, double* v_host) {

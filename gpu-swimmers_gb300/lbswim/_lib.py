@@ -74,6 +74,7 @@ _PROTOS = {
     "lbswim_lattice_set_compat": (C.c_int, [_VP, C.c_int]),
     "lbswim_lattice_set_stream": (C.c_int, [_VP, _VP]),
     "lbswim_lattice_synchronize": (C.c_int, [_VP]),
+    "lbswim_lattice_join": (C.c_int, [_VP]),
     "lbswim_lattice_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP), C.POINTER(C.c_int)]),
     "lbswim_lattice_set_timing": (C.c_int, [_VP, C.c_int]),
     "lbswim_lattice_get_timing": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),

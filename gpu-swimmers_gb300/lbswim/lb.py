@@ -200,6 +200,11 @@ class Lattice:
     def synchronize(self):
         _lib.check(_lib.lib.lbswim_lattice_synchronize(self._h))
 
+    def join(self):
+        """Order this lattice's stream after the tracer moves that System.Step
+        leaves running on the tracers' own streams (no host wait)."""
+        _lib.check(_lib.lib.lbswim_lattice_join(self._h))
+
     def set_timing(self, enable=True):
         """Bracket every LB step kernel of this lattice with CUDA events."""
         _lib.check(_lib.lib.lbswim_lattice_set_timing(self._h, int(bool(enable))))

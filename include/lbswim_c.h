@@ -143,7 +143,12 @@ int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out);
 /* No reference counterpart: behaviour switches and stream binding. */
 int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags);
 int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
+/* synchronize waits on the host for all work on this lattice, including
+ * tracer moves that lbswim_system_step left running on the tracers' own
+ * streams.  join only orders the lattice's stream after that work (no host
+ * wait), e.g. before recording a CUDA event on that stream. */
 int lbswim_lattice_synchronize(lbswim_lattice* lat);
+int lbswim_lattice_join(lbswim_lattice* lat);
 /* Device address and element size of a field's current buffer: 8 (FP64
  * lattices); for FP32/BF16/FP16 lattices fOld/fNew are 4 or 2 bytes, force 4,
  * and rho and u share one buffer of float4 {ux, uy, uz, rho} per site (16). */
@@ -233,7 +238,10 @@ int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
 /* ---- coupled step (System.Step, System.py:9-16) ---------------------------- */
 /* nsteps repetitions of: ZeroForce; AddForces for every swimmer array; Step;
  * CalcHydro; Move for every swimmer array, then every tracer array.  Results
- * are those of the same sequence of single calls. */
+ * are those of the same sequence of single calls.  Tracer moves run on the
+ * tracers' own streams, ordered by events, and may still be running when the
+ * call returns; every other lbswim call on these objects orders itself after
+ * them. */
 int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, int n_swimmers,
                        lbswim_tracers* const* tracers, int n_tracers, int nsteps);
 
