@@ -668,19 +668,22 @@ __global__ void k_rng_draws(unsigned long long seed, int n, unsigned long long s
 
 // ---- FP32-path Move kernels ------------------------------------------------------
 // A block moves NP particles in three phases.  (1) One thread per particle forms
-// its stencil -- wrapped node offsets and Peskin weights -- in shared memory.
-// (2) Sixteen threads per particle gather the 4^3 nodes: lane (y node, z node)
-// of the group loads the four x nodes, and the sixteen partial sums are added
-// with a fixed shuffle tree, so the result does not depend on scheduling.
-// (3) One thread per particle updates it.  GB300's FP64 pipe is narrow, so the
-// FP64 work of phases 1 and 3 is issued once per 32 particles and the stencil
-// origin comes from the bits of the position with integer operations.
+// its stencil -- wrapped origin node and Peskin weights -- in shared memory.
+// (2) A group of 4 (or 8, 16) threads per interpolation point gathers the 4^3
+// nodes, lane k taking z node k & 3, and the partial sums are added with a
+// fixed shuffle tree, so the result does not depend on scheduling.  (3) One
+// thread per particle updates it.  GB300's FP64 pipe is narrow: the stencil
+// origin comes from the bits of the position by integer operations, positions
+// advance in Q44 fixed point, and orientations update in FP32.
 
-// Stencil of one interpolation point: wrapped origin node and Peskin weights.
-struct Stencil {
-  int o[3];
-  int active;  // 0: not gathered
-  float wx[4], wy[4], wz[4];
+// Stencils of NP interpolation points in shared memory, one array per field so
+// that one thread per point writes them without bank conflicts: wrapped origin
+// node, whether the point is gathered, Peskin weights per axis and node.
+template <int NP>
+struct StencilSet {
+  int o[3][NP];
+  int active[NP];
+  float w[3][4][NP];
 };
 
 // x0 = ceil(x - 2) and dr = (float)(x - x0) for one coordinate, with the
@@ -825,20 +828,20 @@ __device__ __forceinline__ void rng_normal3_f(uint64_t seed, uint32_t swimmer, u
   g[2] = r2 * c2;
 }
 
-__device__ __forceinline__ void point_stencil(const Dims& D, const double r[3], Stencil& st) {
+template <int NP>
+__device__ __forceinline__ void point_stencil(const Dims& D, const double r[3],
+                                              StencilSet<NP>& st, int p) {
   float dr[3];
   for (int d = 0; d < 3; ++d) {
     int x0;
     stencil_axis(r[d], x0, dr[d]);
-    st.o[d] = wrap_any(x0, D.n[d]);
+    st.o[d][p] = wrap_any(x0, D.n[d]);
   }
-  st.active = 1;
+  st.active[p] = 1;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    st.wx[j] = peskin_delta<float>(dr[0] - (float)j);
-    st.wy[j] = peskin_delta<float>(dr[1] - (float)j);
-    st.wz[j] = peskin_delta<float>(dr[2] - (float)j);
-  }
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) st.w[d][j][p] = peskin_delta<float>(dr[d] - (float)j);
 }
 
 __device__ __forceinline__ int node_after(int o, int j, int n) {
@@ -847,46 +850,65 @@ __device__ __forceinline__ int node_after(int o, int j, int n) {
   return t;
 }
 
-__device__ __forceinline__ void reduce16(float& vx, float& vy, float& vz) {
+// Sum over the L lanes of a point's group (fixed shuffle tree).
+template <int L>
+__device__ __forceinline__ void reduce_lanes(float& vx, float& vy, float& vz) {
 #pragma unroll
-  for (int off = 8; off > 0; off >>= 1) {
+  for (int off = L / 2; off > 0; off >>= 1) {
     vx += __shfl_xor_sync(0xffffffffu, vx, off);
     vy += __shfl_xor_sync(0xffffffffu, vy, off);
     vz += __shfl_xor_sync(0xffffffffu, vz, off);
   }
 }
 
+// Lane `sub` of the L lanes (4, 8 or 16) of a point gathers z node sub & 3 of
+// y nodes sub >> 2, sub >> 2 + L / 4, ... for the four x nodes.
+template <int L, int NP>
 __device__ __forceinline__ void gather_point(const float4* __restrict__ h, const Dims& D,
-                                             const Stencil& s, int jy, int kz, float& vx,
-                                             float& vy, float& vz) {
+                                             const StencilSet<NP>& s, int p, int sub,
+                                             float& vx, float& vy, float& vz) {
   vx = vy = vz = 0.f;
-  if (!s.active) return;
+  if (!s.active[p]) return;
   const int nz = D.n[2], nynz = D.n[1] * D.n[2];
-  const int yz = node_after(s.o[1], jy, D.n[1]) * nz + node_after(s.o[2], kz, nz);
-  const float wyz = s.wy[jy] * s.wz[kz];
+  const int kz = sub & 3;
+  const int z = node_after(s.o[2][p], kz, nz);
+  const float wz = s.w[2][kz][p];
+  int xo[4];
+  float wx[4];
 #pragma unroll
   for (int ix = 0; ix < 4; ++ix) {
-    const float4 q = __ldg(h + node_after(s.o[0], ix, D.n[0]) * nynz + yz);
-    const float w = s.wx[ix] * wyz;
-    vx += w * q.x;
-    vy += w * q.y;
-    vz += w * q.z;
+    xo[ix] = node_after(s.o[0][p], ix, D.n[0]) * nynz;
+    wx[ix] = s.w[0][ix][p];
+  }
+#pragma unroll
+  for (int jy = sub >> 2; jy < 4; jy += L / 4) {
+    const int yz = node_after(s.o[1][p], jy, D.n[1]) * nz + z;
+    const float wyz = s.w[1][jy][p] * wz;
+#pragma unroll
+    for (int ix = 0; ix < 4; ++ix) {
+      const float4 q = __ldg(h + xo[ix] + yz);
+      const float w = wx[ix] * wyz;
+      vx += w * q.x;
+      vy += w * q.y;
+      vz += w * q.z;
+    }
   }
 }
 
-// Phase 2: the block's threads, sixteen per point and two points per group at a
-// time, gather the velocity of npts stencils.  Every thread runs the same
-// number of iterations (npts is a multiple of blockDim / 8).
+// Phase 2: the block's threads, L per point and two points per group at a
+// time, gather the velocity of the NP stencils.  Every thread runs the same
+// number of iterations (NP * L is a multiple of 2 * blockDim).
+template <int L, int NP>
 __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const Dims& D,
-                                             const Stencil* st, int npts, float3* vel) {
-  const int sub = threadIdx.x & 15, jy = sub >> 2, kz = sub & 3;
-  const int groups = blockDim.x >> 4;
-  for (int p = threadIdx.x >> 4; p < npts; p += 2 * groups) {
+                                             const StencilSet<NP>& st, float3* vel) {
+  const int sub = threadIdx.x & (L - 1);
+  const int groups = blockDim.x / L;
+  for (int p = threadIdx.x / L; p < NP; p += 2 * groups) {
     float ax, ay, az, bx, by, bz;
-    gather_point(h, D, st[p], jy, kz, ax, ay, az);
-    gather_point(h, D, st[p + groups], jy, kz, bx, by, bz);
-    reduce16(ax, ay, az);
-    reduce16(bx, by, bz);
+    gather_point<L>(h, D, st, p, sub, ax, ay, az);
+    gather_point<L>(h, D, st, p + groups, sub, bx, by, bz);
+    reduce_lanes<L>(ax, ay, az);
+    reduce_lanes<L>(bx, by, bz);
     if (sub == 0) {
       vel[p] = make_float3(ax, ay, az);
       vel[p + groups] = make_float3(bx, by, bz);
@@ -895,23 +917,24 @@ __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const
 }
 
 constexpr int TRACER_MOVE_BLOCK = 256;
+constexpr int TRACER_LANES = 4;  // lanes per interpolation point
 
 __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
     int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
     const float4* __restrict__ h) {
-  __shared__ Stencil st[TRACER_MOVE_BLOCK];
+  __shared__ StencilSet<TRACER_MOVE_BLOCK> st;
   __shared__ float3 vel[TRACER_MOVE_BLOCK];
   const int i = blockIdx.x * TRACER_MOVE_BLOCK + threadIdx.x;
   const bool valid = i < ntr;
   double rr[3] = {0.0, 0.0, 0.0};
   if (valid) {
     for (int d = 0; d < 3; ++d) rr[d] = r[(long long)ntr * d + i];
-    point_stencil(D, rr, st[threadIdx.x]);
+    point_stencil(D, rr, st, threadIdx.x);
   } else {
-    st[threadIdx.x].active = 0;
+    st.active[threadIdx.x] = 0;
   }
   __syncthreads();
-  gather_block(h, D, st, TRACER_MOVE_BLOCK, vel);
+  gather_block<TRACER_LANES>(h, D, st, vel);
   __syncthreads();
   if (!valid) return;
   const float3 w = vel[threadIdx.x];
@@ -924,10 +947,11 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
   }
 }
 
-// Swimmers are few, so a block takes 16 of them on 256 threads: two stencils
-// (front and rear point) per swimmer, 16 threads per stencil.
-constexpr int SWIMMER_MOVE_BLOCK = 256;
-constexpr int SWIMMERS_PER_BLOCK = 16;
+// A block takes SWIMMERS_PER_BLOCK swimmers: two stencils (front and rear
+// point) per swimmer, SWIMMER_LANES threads per stencil.
+constexpr int SWIMMERS_PER_BLOCK = 64;
+constexpr int SWIMMER_LANES = 4;  // lanes per interpolation point
+constexpr int SWIMMER_MOVE_BLOCK = SWIMMERS_PER_BLOCK * SWIMMER_LANES;
 
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
@@ -935,7 +959,7 @@ __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     const float4* __restrict__ h) {
   constexpr int B = SWIMMERS_PER_BLOCK;
   // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
-  __shared__ Stencil st[2 * B];
+  __shared__ StencilSet<2 * B> st;
   __shared__ float3 vel[2 * B];
   const int t = threadIdx.x, i = blockIdx.x * B + t;
   const bool mine = t < B, valid = mine && i < nsw;
@@ -951,19 +975,19 @@ __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     }
     tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
     rotate = !tumble && !c.rotational_advection_off;
-    point_stencil(D, r, st[t]);
+    point_stencil(D, r, st, t);
     if (rotate) {
       for (int d = 0; d < 3; ++d) rMinus[d] = r[d] - nd[d] * c.l;
-      point_stencil(D, rMinus, st[B + t]);
+      point_stencil(D, rMinus, st, B + t);
     } else {
-      st[B + t].active = 0;
+      st.active[B + t] = 0;
     }
   } else if (mine) {
-    st[t].active = 0;
-    st[B + t].active = 0;
+    st.active[t] = 0;
+    st.active[B + t] = 0;
   }
   __syncthreads();
-  gather_block(h, D, st, 2 * B, vel);
+  gather_block<SWIMMER_LANES>(h, D, st, vel);
   __syncthreads();
   if (!valid) return;
   const float3 w = vel[t], wm = vel[B + t];
