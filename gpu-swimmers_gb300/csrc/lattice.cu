@@ -350,7 +350,7 @@ __host__ __device__ constexpr int ring_pop_planes() {
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
 // Shared-memory layout of the SPREAD instances after the ring: fixed-point
-// force sums of one plane [3][PLANE] (int64), coverage masks [CAP] (u64), ends
+// force sums of one plane as 32-bit halves [3][lo, hi][PLANE], coverage masks [CAP] (u64), ends
 // [CAP], local node rows [CAP], per-plane list offsets [LX + 3], lists.
 template <int TZ, int TY>
 struct SpreadLayout {
@@ -362,7 +362,7 @@ struct SpreadLayout {
   static constexpr int nodes = align16(ends + SPREAD_CAP * (int)sizeof(SlabEnd));
   static constexpr int poff = align16(nodes + SPREAD_CAP * (int)sizeof(NodeLocal));
   static constexpr int plist = align16(poff + (FUSED_LX + 3) * 4);
-  static constexpr int total = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END);
+  static constexpr int total = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END * 2);
 };
 
 template <int TZ, int TY, bool SPREAD>
@@ -416,15 +416,20 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
 
   // ---- this slab's pending dipole ends and the fixed-point force plane ----
   using SL = SpreadLayout<TZ, TY>;
-  long long* fq = reinterpret_cast<long long*>(smraw + SL::fq);  // [3][PLANE]
+  // 64-bit fixed-point sums kept as 32-bit halves [3][lo, hi][PLANE]: 32-bit
+  // shared-memory atomics are native, 64-bit ones are not
+  unsigned* fq = reinterpret_cast<unsigned*>(smraw + SL::fq);
   // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 63;
   // bit 63: a node of end q appears twice in the cross-section (tiny lattices)
   unsigned long long* xmask = reinterpret_cast<unsigned long long*>(smraw + SL::xmask);
   SlabEnd* srec = reinterpret_cast<SlabEnd*>(smraw + SL::ends);
   NodeLocal* nodes = reinterpret_cast<NodeLocal*>(smraw + SL::nodes);
-  // ends covering each local plane: plist[poff[kk] .. poff[kk + 1]) (indices into srec)
+  // ends covering each local plane: plist[poff[kk] .. poff[kk + 1]), entries
+  // q | ix << 8 | flags (q indexes srec, ix is the x node on the plane)
   int* poff = reinterpret_cast<int*>(smraw + SL::poff);
-  unsigned char* plist = smraw + SL::plist;
+  unsigned short* plist = reinterpret_cast<unsigned short*>(smraw + SL::plist);
+  constexpr unsigned PL_FOLD = 1u << 10;  // nx < 4: several x nodes fold onto the plane
+  constexpr unsigned PL_DUP = 1u << 11;   // a node appears twice in the cross-section
   const float fx_scale = SPREAD ? a.fixed_scale[0] : 0.f;
   const float fx_inv = SPREAD ? a.fixed_scale[1] : 0.f;
   int cnt = 0;
@@ -463,7 +468,7 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
         xmask[q] = m;
       }
     }
-    for (int i = tid; i < 3 * PLANE; i += blockDim.x) fq[i] = 0;
+    for (int i = tid; i < 3 * 2 * PLANE; i += blockDim.x) fq[i] = 0u;
     __syncthreads();
     if (in_smem) {
       // per-plane lists in increasing end position: count, offsets, fill
@@ -488,7 +493,13 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
           const int q = base + lane;
           const bool cov = q < cnt && ((xmask[q] >> kk) & 1ull);
           const unsigned m = __ballot_sync(0xffffffffu, cov);
-          if (cov) plist[at + __popc(m & ((1u << lane) - 1u))] = (unsigned char)q;
+          if (cov) {
+            int ix = wrap_once(x0 - 1 + kk, nx) - srec[q].ox;
+            if (ix < 0) ix += nx;
+            const unsigned ent = (unsigned)q | (nx >= 4 ? (unsigned)ix << 8 : PL_FOLD) |
+                                 ((xmask[q] >> 63) ? PL_DUP : 0u);
+            plist[at + __popc(m & ((1u << lane) - 1u))] = (unsigned short)ent;
+          }
           at += __popc(m);
         }
       }
@@ -499,27 +510,40 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   // (end, (jy, jz) node) are shared among all threads of the CTA.
   auto scatter_plane = [&](int kk) {
     const int gx = wrap_once(x0 - 1 + kk, nx);
+    // exact 64-bit addition: the low half's carry goes into the high half
+    auto add1 = [&](unsigned* lo, long long q) {
+      const unsigned l = (unsigned)q;
+      const unsigned old = atomicAdd(lo, l);
+      const int h = (int)(q >> 32) + (old + l < old ? 1 : 0);
+      if (h != 0) atomicAdd(reinterpret_cast<int*>(lo + PLANE), h);
+    };
     auto add3 = [&](int at, long long q0, long long q1, long long q2) {
-      atomicAdd(reinterpret_cast<unsigned long long*>(fq + at), (unsigned long long)q0);
-      atomicAdd(reinterpret_cast<unsigned long long*>(fq + PLANE + at), (unsigned long long)q1);
-      atomicAdd(reinterpret_cast<unsigned long long*>(fq + 2 * PLANE + at), (unsigned long long)q2);
+      add1(fq + at, q0);
+      add1(fq + 2 * PLANE + at, q1);
+      add1(fq + 4 * PLANE + at, q2);
     };
     if (in_smem) {
-      // (end, node) pairs of the ends covering this plane, on contiguous threads
+      // (end, node) pairs of the ends covering this plane, on contiguous
+      // threads; the ring threads, which write no output plane, go first
       const int p0 = poff[kk], np = poff[kk + 1] - p0;
-      for (int t = tid; t < np * 16; t += blockDim.x) {
-        const int q = plist[p0 + (t >> 4)];
-        const SlabEnd& e = srec[q];
+      const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
+      for (int t = rt; t < np * 16; t += blockDim.x) {
+        const unsigned ent = plist[p0 + (t >> 4)];
+        const int q = (int)(ent & 0xffu);
         const int jy = (t >> 2) & 3, jz = t & 3;
         const int ly2 = nodes[q].y[jy], lz2 = nodes[q].z[jz];
         if ((ly2 | lz2) < 0) continue;  // node outside this cross-section
+        const SlabEnd& e = srec[q];
         float wx;
-        cover_weight(gx, e.ox, nx, e.phi[0], wx);
+        if (ent & PL_FOLD)
+          cover_weight(gx, e.ox, nx, e.phi[0], wx);
+        else
+          wx = e.phi[0][(ent >> 8) & 3u];
         const float py = e.phi[1][jy], pz = e.phi[2][jz];
         const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
         const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
         const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
-        if (!(xmask[q] >> 63)) {
+        if (!(ent & PL_DUP)) {
           add3(ly2 * HZ + lz2, q0, q1, q2);
         } else {
           // tiny lattice: a node can appear at several places of the cross-section
@@ -574,11 +598,14 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
     if (SPREAD && active) {
       // force = base + spread (k_force_tile writes the same bits)
-      long long* f0 = fq + my;
-      cur[15] += fx_value(f0[0], fx_inv);
-      cur[16] += fx_value(f0[PLANE], fx_inv);
-      cur[17] += fx_value(f0[2 * PLANE], fx_inv);
-      f0[0] = f0[PLANE] = f0[2 * PLANE] = 0;  // ready for plane k + 1
+      unsigned* f0 = fq + my;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long q = (long long)(((unsigned long long)f0[(2 * c + 1) * PLANE] << 32) |
+                                        f0[2 * c * PLANE]);
+        cur[15 + c] += fx_value(q, fx_inv);
+        f0[2 * c * PLANE] = f0[(2 * c + 1) * PLANE] = 0u;  // ready for plane k + 1
+      }
     }
     // ring slots: plane k is written to A[k % NA], B[k % NB], C[k % NC]
     const int wa_slot = SPREAD ? k3 : (k & 3);
