@@ -322,9 +322,10 @@ struct FusedArgs {
   Relax<float> k;
   // pending dipole ends spread by the kernel itself (SPREAD instances)
   const EndRecord<float>* ends;
-  const unsigned* slab_start;
-  const int* slab_list;
-  const float* fixed_scale;  // device: 2^S, 2^-S of the fixed-point force sums
+  const unsigned* slab_count;  // [slabs] ends listed per slab (may exceed the capacity)
+  const int* slab_list;        // [slabs][SLAB_BUCKET_CAP]
+  int npending;
+  const unsigned* max_abs_f;   // device: largest |F| component, as float bits
 };
 
 // Post-collision populations wait in shared memory until the output plane can
@@ -430,16 +431,20 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   unsigned short* plist = reinterpret_cast<unsigned short*>(smraw + SL::plist);
   constexpr unsigned PL_FOLD = 1u << 10;  // nx < 4: several x nodes fold onto the plane
   constexpr unsigned PL_DUP = 1u << 11;   // a node appears twice in the cross-section
-  const float fx_scale = SPREAD ? a.fixed_scale[0] : 0.f;
-  const float fx_inv = SPREAD ? a.fixed_scale[1] : 0.f;
+  const int fx_exp = SPREAD ? fixed_scale_exp(a.npending, *a.max_abs_f) : 0;
+  const float fx_scale = SPREAD ? exp2_int(fx_exp) : 0.f;
+  const float fx_inv = SPREAD ? exp2_int(-fx_exp) : 0.f;
   int cnt = 0;
-  unsigned s0 = 0;
-  bool in_smem = true;
+  long long s0 = 0;
+  bool in_smem = true, overflow = false;
   if (SPREAD) {
     const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    s0 = a.slab_start[slab];
-    cnt = (int)(a.slab_start[slab + 1] - s0);
-    in_smem = cnt <= SPREAD_CAP;
+    const unsigned c = a.slab_count[slab];
+    // a slab whose bucket overflowed is spread from the whole list of ends
+    overflow = c > (unsigned)SLAB_BUCKET_CAP;
+    cnt = overflow ? a.npending : (int)c;
+    s0 = (long long)slab * SLAB_BUCKET_CAP;
+    in_smem = !overflow && cnt <= SPREAD_CAP;
     if (in_smem) {
       for (int q = tid; q < cnt; q += blockDim.x) {
         const EndRecord<float>& g = a.ends[a.slab_list[s0 + q]];
@@ -554,7 +559,7 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     } else {
       // more ends than shared memory holds: every end, records from global memory
       for (int t = tid; t < cnt * 16; t += blockDim.x) {
-        const EndRecord<float>& e = a.ends[a.slab_list[s0 + (t >> 4)]];
+        const EndRecord<float>& e = a.ends[overflow ? (t >> 4) : a.slab_list[s0 + (t >> 4)]];
         float wx;
         if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
         const int jy = (t >> 2) & 3, jz = t & 3;
@@ -787,15 +792,22 @@ static void launch_fused(Lattice* L, const FusedArgs& a) {
 template <class S, int TZ, int TY>
 static void fused_step_tile(Lattice* L, FusedArgs& a) {
   if (L->spread.pending > 0) {
-    const SlabSpread sp = spread_prepare_slabs(L, FUSED_LX, TY, TZ);
+    const SlabSpread sp = spread_prepare_slabs(L);
     a.ends = (const EndRecord<float>*)sp.ends;
-    a.slab_start = sp.start;
+    a.slab_count = sp.count;
     a.slab_list = sp.list;
-    a.fixed_scale = sp.fixed_scale;
+    a.npending = sp.npending;
+    a.max_abs_f = sp.max_abs_force;
     launch_fused<S, TZ, TY, true>(L, a);
   } else {
     launch_fused<S, TZ, TY, false>(L, a);
   }
+}
+
+void fused_slab_shape(const Lattice* L, int T[3]) {
+  T[0] = FUSED_LX;
+  T[1] = L->fused_tile == 1 ? 16 : 8;
+  T[2] = L->fused_tile == 1 ? 16 : 32;
 }
 
 template <class S>

@@ -8,6 +8,7 @@
 // transform (lb.cu:114-119, 198-203) with the zero entries and the zeroed
 // ghost modes (lb.cu:191-195) taken out: f_p = w_p (rho + 3 c_p.j + 9/2 Q_p:S).
 #pragma once
+#include <cstring>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -273,6 +274,75 @@ __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : 
 __device__ __forceinline__ int wrap_any(int i, int n) {
   i %= n;
   return i < 0 ? i + n : i;
+}
+
+// x0 = ceil(x - 2) and dr = (float)(x - x0) for one coordinate, with the
+// rounding of those FP64 operations.  For 0 <= x < 2^30 both come from the
+// bits of x by integer operations: x - x0 is exact in FP64 unless x < 1, where
+// 1 + x is first rounded to FP64's 52 fraction bits, then to FP32's 23.  Other
+// values take FP64.
+__device__ __forceinline__ void stencil_axis(double x, int& x0, float& dr) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)(b >> 52);  // biased exponent; negative x gives ex >= 2048
+  if (ex >= 1023 + 30) {
+    const double c = ceil(x - 2.);
+    x0 = (int)c;
+    dr = (float)(x - c);
+    return;
+  }
+  if (ex < 1023 - 40) {  // 0 <= x < 2^-40: x - 2 rounds to -2 when x <= 2^-53
+    const bool low = b <= (970ull << 52);
+    x0 = low ? -2 : -1;
+    dr = low ? 2.f : 1.f;
+    return;
+  }
+  const unsigned long long mant = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int shift = 1075 - ex;  // x = mant * 2^-shift, 23 <= shift <= 92
+  unsigned long long f52;       // fraction of x - x0 in 2^-52 units
+  if (shift <= 52) {
+    const unsigned long long fr = mant & ((1ull << shift) - 1);
+    const int cell = (int)(mant >> shift);
+    if (fr == 0) {  // x is an integer
+      x0 = cell - 2;
+      dr = 2.f;
+      return;
+    }
+    x0 = cell - 1;
+    f52 = fr << (52 - shift);
+  } else {  // 2^-40 <= x < 1
+    x0 = -1;
+    const int s = shift - 52;  // 1 .. 40
+    const unsigned long long rem = mant & ((1ull << s) - 1), half = 1ull << (s - 1);
+    f52 = mant >> s;
+    f52 += (rem > half || (rem == half && (f52 & 1ull))) ? 1ull : 0ull;
+  }
+  // to 23 fraction bits; a carry out gives 2.0f
+  unsigned m = (unsigned)(f52 >> 29);
+  const unsigned rem = (unsigned)(f52 & 0x1fffffffull);
+  m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  dr = __int_as_float(0x3f800000 + (int)m);
+}
+
+// Exponent S of the fixed-point force sums (scale 2^S) for `npending` dipole
+// ends whose largest force component is the float with bits `max_bits`: the
+// sum of all their contributions stays below 2^61 in magnitude.  Integer and
+// FP32 operations only, so every kernel that spreads derives the same S.
+__host__ __device__ inline int fixed_scale_exp(int npending, unsigned max_bits) {
+  float m;
+  memcpy(&m, &max_bits, sizeof(float));
+  if (!(m > 0.f) || npending <= 0) return 60;
+  const float b = (float)npending * m * 1.00000095367431640625f;  // 1 + 2^-20 covers rounding
+  unsigned bb;
+  memcpy(&bb, &b, sizeof(float));
+  const int e = (int)((bb >> 23) & 0xffu) - 127;  // floor(log2 b) for a normal b
+  const int S = 60 - e;
+  return S < -100 ? -100 : (S > 100 ? 100 : S);
+}
+__host__ __device__ inline float exp2_int(int S) {  // 2^S for -126 <= S <= 127
+  const unsigned u = (unsigned)(S + 127) << 23;
+  float f;
+  memcpy(&f, &u, sizeof(float));
+  return f;
 }
 
 // ---- dipole ends of the force spreading (SwimmerArray.cu:42-112) ---------------

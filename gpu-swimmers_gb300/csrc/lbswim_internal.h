@@ -59,6 +59,10 @@ struct TileLists {
 // the dense buffer at once; reduced-precision lattices keep them pending and
 // the step kernel spreads them itself, so the force never goes through HBM
 // unless someone reads it.
+// Ends listed per step-kernel slab, at most SLAB_BUCKET_CAP per slab (a slab
+// with more is spread from the whole list of pending ends).
+constexpr int SLAB_BUCKET_CAP = 1024;
+
 struct SpreadScratch {
   int capacity_ends = 0;
   void* ends = nullptr;  // [capacity_ends] EndRecord of the pending ends
@@ -66,17 +70,21 @@ struct SpreadScratch {
   int pending = 0;
   bool stepped = false;  // a Step already consumed the pending ends
   unsigned* max_abs_force = nullptr;  // device: largest |F| component of the pending ends
-  float* fixed_scale = nullptr;       // device: 2^S and 2^-S of the fixed-point sums
   TileLists ftiles;      // force tiles, for materialisation
-  TileLists slabs;       // step-kernel slabs
+  // slab buckets of the pending ends, filled as the ends are recorded
+  unsigned* bucket_count = nullptr;  // [bucket_slabs]
+  int* bucket_list = nullptr;        // [bucket_slabs][SLAB_BUCKET_CAP]
+  int bucket_slabs = 0;
+  int bucket_tile = -1;  // slab shape the buckets hold (Lattice::fused_tile), -1: stale
 };
 
 // What the fused step kernel needs to spread the pending ends itself.
 struct SlabSpread {
   const void* ends = nullptr;
-  const unsigned* start = nullptr;
+  const unsigned* count = nullptr;
   const int* list = nullptr;
-  const float* fixed_scale = nullptr;
+  int npending = 0;
+  const unsigned* max_abs_force = nullptr;
 };
 
 struct Lattice {
@@ -178,7 +186,10 @@ inline void lattice_join(Lattice* L) { lattice_wait_readers(L, nullptr); }
 
 // particles.cu: force spreading state
 void spread_materialise(Lattice* L);
-SlabSpread spread_prepare_slabs(Lattice* L, int LX, int TY, int TZ);
+SlabSpread spread_prepare_slabs(Lattice* L);
+// Slab shape of the fused step kernel for a lattice: x planes per slab, rows,
+// columns (lattice.cu).
+void fused_slab_shape(const Lattice* L, int T[3]);
 void spread_free(SpreadScratch& S);
 
 // particles.cu

@@ -277,12 +277,38 @@ constexpr int REC_THREADS = 256;
 
 // One record per dipole end: e = 2i is the tail, 2i + 1 the head.  Records are
 // assembled in shared memory and written out as one contiguous block.
+// List end e under every slab of grid G whose extended region its stencil
+// touches (at most SLAB_BUCKET_CAP ends are kept per slab; the count goes on).
+__device__ __forceinline__ void bucket_end(int e, const int o[3], const Dims& D, const TileGrid& G,
+                                           unsigned* __restrict__ count,
+                                           int* __restrict__ list) {
+  int f[3], c[3];
+  for (int a = 0; a < 3; ++a) touched_range(o[a], D.n[a], G.T[a], G.h, G.nt[a], f[a], c[a]);
+  for (int i = 0; i < c[0]; ++i) {
+    const int kx = f[0] + i < G.nt[0] ? f[0] + i : f[0] + i - G.nt[0];
+    for (int j = 0; j < c[1]; ++j) {
+      const int ky = f[1] + j < G.nt[1] ? f[1] + j : f[1] + j - G.nt[1];
+      for (int k = 0; k < c[2]; ++k) {
+        const int kz = f[2] + k < G.nt[2] ? f[2] + k : f[2] + k - G.nt[2];
+        const int t = (kx * G.nt[1] + ky) * G.nt[2] + kz;
+        const unsigned slot = atomicAdd(count + t, 1u);
+        if (slot < (unsigned)SLAB_BUCKET_CAP) list[(long long)t * SLAB_BUCKET_CAP + slot] = e;
+      }
+    }
+  }
+}
+
+// One record per dipole end: e = 2i is the tail, 2i + 1 the head.  Records are
+// assembled in shared memory and written out as one contiguous block; with
+// bucket_count set, each end is also listed under the step-kernel slabs it
+// touches (its index among all pending ends is e_base + e).  FP32 records take
+// the stencil origin from the bits of the position (stencil_axis) and the
+// weights of dr - i, like the FP32 interpolation.
 template <class T>
-__global__ void __launch_bounds__(REC_THREADS) k_end_records(int nsw, const double* __restrict__ r,
-                                                             const double* __restrict__ nv,
-                                                             double P, double l, Dims D,
-                                                             EndRecord<T>* __restrict__ ends,
-                                                             unsigned* __restrict__ max_abs_f) {
+__global__ void __launch_bounds__(REC_THREADS) k_end_records(
+    int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P, double l,
+    Dims D, EndRecord<T>* __restrict__ ends, int e_base, unsigned* __restrict__ max_abs_f,
+    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list) {
   __shared__ EndRecord<T> srec[REC_THREADS];
   __shared__ unsigned smax;
   if (threadIdx.x == 0) smax = 0u;
@@ -301,7 +327,18 @@ __global__ void __launch_bounds__(REC_THREADS) k_end_records(int nsw, const doub
       if (head) F[a] *= -1.0;
     }
     EndRecord<T>& rec = srec[threadIdx.x];
-    stencil_setup<T>(D, rr, rec.o, rec.phi);
+    if constexpr (sizeof(T) == 4) {
+      for (int a = 0; a < 3; ++a) {
+        int x0;
+        float dr;
+        stencil_axis(rr[a], x0, dr);
+        rec.o[a] = wrap_any(x0, D.n[a]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) rec.phi[a][j] = peskin_delta<float>(dr - (float)j);
+      }
+    } else {
+      stencil_setup<T>(D, rr, rec.o, rec.phi);
+    }
     rec.pad = 0;
     float m = 0.f;
     for (int a = 0; a < 3; ++a) {
@@ -310,6 +347,7 @@ __global__ void __launch_bounds__(REC_THREADS) k_end_records(int nsw, const doub
     }
     // non-negative floats order like their bit patterns
     atomicMax(&smax, __float_as_uint(m));
+    if (bucket_count) bucket_end(e_base + e, rec.o, D, G, bucket_count, bucket_list);
   }
   __syncthreads();
   if (threadIdx.x == 0 && max_abs_f) atomicMax(max_abs_f, smax);
@@ -320,7 +358,15 @@ __global__ void __launch_bounds__(REC_THREADS) k_end_records(int nsw, const doub
   for (int w = threadIdx.x; w < words; w += REC_THREADS) dst[w] = src[w];
 }
 
-// pass 0 counts, pass 1 scatters end ids into the tile lists.
+// Slab buckets of recorded ends (the slab shape changed since they were recorded).
+__global__ void k_bucket_ends(int nends, const EndRecord<float>* __restrict__ ends, Dims D,
+                              TileGrid G, unsigned* __restrict__ count, int* __restrict__ list) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nends) return;
+  const int o[3] = {ends[e].o[0], ends[e].o[1], ends[e].o[2]};
+  bucket_end(e, o, D, G, count, list);
+}
+
 template <class T, int PASS>
 __global__ void k_touch(int nends, const EndRecord<T>* __restrict__ ends, Dims D, TileGrid G,
                         unsigned* __restrict__ count, const unsigned* __restrict__ start,
@@ -372,21 +418,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply_total(
   }
 }
 
-// 2^S with S the largest power keeping every fixed-point site sum below 2^61: a
-// site's contributions add up to at most (number of ends) x (largest |F|).
-__global__ void k_fx_scale(int npending, const unsigned* __restrict__ max_abs_f,
-                           float* __restrict__ out) {
-  const float m = __uint_as_float(*max_abs_f);
-  int S = 60;
-  if (m > 0.f && npending > 0) {
-    const double bound = (double)npending * (double)m * 1.0000001;
-    S = (int)floor(61.0 - log2(bound));
-  }
-  S = max(-100, min(100, S));
-  out[0] = ldexpf(1.0f, S);
-  out[1] = ldexpf(1.0f, -S);
-}
-
 // Force tile: 8 (x) x 8 (y) x 32 (z) sites, 16 warps, each warp owns 4 of the 64
 // z-rows; a warp ballot picks the ends covering a row.
 //  * FP64: the ends are put in end order by rank and every site adds their
@@ -402,7 +433,8 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
                                                            const unsigned* __restrict__ start,
                                                            const int* __restrict__ list,
                                                            int* __restrict__ sorted,
-                                                           const float* __restrict__ fixed_scale,
+                                                           int npending,
+                                                           const unsigned* __restrict__ max_abs_f,
                                                            T* __restrict__ force, int accumulate) {
   constexpr bool FIXED = sizeof(T) == 4;
   __shared__ EndRecord<T> srec[FT_CAP];
@@ -434,7 +466,8 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
   auto rec = [&](int q) -> const EndRecord<T>& {
     return in_smem ? srec[q] : ends[FIXED ? list[s0 + q] : sorted[s0 + q]];
   };
-  const float fx_scale = FIXED ? fixed_scale[0] : 0.f, fx_inv = FIXED ? fixed_scale[1] : 0.f;
+  const int fx_exp = FIXED ? fixed_scale_exp(npending, *max_abs_f) : 0;
+  const float fx_scale = FIXED ? exp2_int(fx_exp) : 0.f, fx_inv = FIXED ? exp2_int(-fx_exp) : 0.f;
   const int z = kz * FT_Z + lane;
   const bool zval = z < D.n[2];
   for (int row = warp; row < FT_X * FT_Y; row += FT_THREADS / 32) {
@@ -685,53 +718,6 @@ struct StencilSet {
   int active[NP];
   float w[3][4][NP];
 };
-
-// x0 = ceil(x - 2) and dr = (float)(x - x0) for one coordinate, with the
-// rounding of those FP64 operations.  For 0 <= x < 2^30 both come from the
-// bits of x by integer operations: x - x0 is exact in FP64 unless x < 1, where
-// 1 + x is first rounded to FP64's 52 fraction bits, then to FP32's 23.  Other
-// values take FP64.
-__device__ __forceinline__ void stencil_axis(double x, int& x0, float& dr) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int ex = (int)(b >> 52);  // biased exponent; negative x gives ex >= 2048
-  if (ex >= 1023 + 30) {
-    const double c = ceil(x - 2.);
-    x0 = (int)c;
-    dr = (float)(x - c);
-    return;
-  }
-  if (ex < 1023 - 40) {  // 0 <= x < 2^-40: x - 2 rounds to -2 when x <= 2^-53
-    const bool low = b <= (970ull << 52);
-    x0 = low ? -2 : -1;
-    dr = low ? 2.f : 1.f;
-    return;
-  }
-  const unsigned long long mant = (b & 0xfffffffffffffull) | (1ull << 52);
-  const int shift = 1075 - ex;  // x = mant * 2^-shift, 23 <= shift <= 92
-  unsigned long long f52;       // fraction of x - x0 in 2^-52 units
-  if (shift <= 52) {
-    const unsigned long long fr = mant & ((1ull << shift) - 1);
-    const int cell = (int)(mant >> shift);
-    if (fr == 0) {  // x is an integer
-      x0 = cell - 2;
-      dr = 2.f;
-      return;
-    }
-    x0 = cell - 1;
-    f52 = fr << (52 - shift);
-  } else {  // 2^-40 <= x < 1
-    x0 = -1;
-    const int s = shift - 52;  // 1 .. 40
-    const unsigned long long rem = mant & ((1ull << s) - 1), half = 1ull << (s - 1);
-    f52 = mant >> s;
-    f52 += (rem > half || (rem == half && (f52 & 1ull))) ? 1ull : 0ull;
-  }
-  // to 23 fraction bits; a carry out gives 2.0f
-  unsigned m = (unsigned)(f52 >> 29);
-  const unsigned rem = (unsigned)(f52 & 0x1fffffffull);
-  m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
-  dr = __int_as_float(0x3f800000 + (int)m);
-}
 
 // Exact FP64 value of a float, from its bits (no FP64 instruction).
 __device__ __forceinline__ double f2d_exact(float f) {
@@ -1053,12 +1039,15 @@ static void free_lists(TileLists& TL) {
 void spread_free(SpreadScratch& S) {
   if (S.ends) cudaFree(S.ends);
   if (S.max_abs_force) cudaFree(S.max_abs_force);
-  if (S.fixed_scale) cudaFree(S.fixed_scale);
+  if (S.bucket_count) cudaFree(S.bucket_count);
+  if (S.bucket_list) cudaFree(S.bucket_list);
   S.ends = nullptr;
   S.max_abs_force = nullptr;
-  S.fixed_scale = nullptr;
+  S.bucket_count = nullptr;
+  S.bucket_list = nullptr;
+  S.bucket_slabs = 0;
+  S.bucket_tile = -1;
   free_lists(S.ftiles);
-  free_lists(S.slabs);
 }
 
 static size_t record_bytes(const Lattice* L) {
@@ -1142,12 +1131,6 @@ static void bin_ends(Lattice* L, TileLists& TL, const TileGrid& G) {
 
 // Fold the pending ends into the dense force buffer (force = base + spread).
 // 2^S for the fixed-point sums of the pending ends, computed on the device.
-static const float* fixed_scale_for_pending(Lattice* L) {
-  SpreadScratch& S = L->spread;
-  k_fx_scale<<<1, 1, 0, L->stream>>>(S.pending, S.max_abs_force, S.fixed_scale);
-  LB_CHECK_LAUNCH(1);
-  return S.fixed_scale;
-}
 
 template <class T>
 static void materialise_t(Lattice* L) {
@@ -1155,10 +1138,9 @@ static void materialise_t(Lattice* L) {
   const TileGrid G = force_tiles(L);
   bin_ends<T>(L, S.ftiles, G);
   const Dims D = make_dims(L);
-  const float* fs = sizeof(T) == 4 ? fixed_scale_for_pending(L) : nullptr;
   k_force_tile<T><<<S.ftiles.ntiles, FT_THREADS, 0, L->stream>>>(
-      D, G, (const EndRecord<T>*)S.ends, S.ftiles.start, S.ftiles.list, S.ftiles.sorted, fs,
-      (T*)L->force, L->force_zero_pending ? 0 : 1);
+      D, G, (const EndRecord<T>*)S.ends, S.ftiles.start, S.ftiles.list, S.ftiles.sorted,
+      S.pending, S.max_abs_force, (T*)L->force, L->force_zero_pending ? 0 : 1);
   LB_CHECK_LAUNCH(1);
   S.pending = 0;
   S.stepped = false;
@@ -1176,20 +1158,52 @@ void spread_materialise(Lattice* L) {
   }
 }
 
-SlabSpread spread_prepare_slabs(Lattice* L, int LX, int TY, int TZ) {
-  SpreadScratch& S = L->spread;
+static TileGrid slab_grid(const Lattice* L) {
   TileGrid G;
-  G.T[0] = LX;
-  G.T[1] = TY;
-  G.T[2] = TZ;
+  fused_slab_shape(L, G.T);
   G.h = 1;  // the step kernel collides a one-site ring around its slab
   for (int a = 0; a < 3; ++a) G.nt[a] = (L->size[a] + G.T[a] - 1) / G.T[a];
-  bin_ends<float>(L, S.slabs, G);
+  return G;
+}
+
+// Bucket storage for the current slab grid; false when it had to be replaced
+// (the buckets are then stale).
+static bool ensure_buckets(Lattice* L) {
+  SpreadScratch& S = L->spread;
+  const TileGrid G = slab_grid(L);
+  const int nslabs = G.nt[0] * G.nt[1] * G.nt[2];
+  if (S.bucket_slabs == nslabs && S.bucket_count) return true;
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  if (S.bucket_count) cudaFree(S.bucket_count);
+  if (S.bucket_list) cudaFree(S.bucket_list);
+  S.bucket_count = nullptr;
+  S.bucket_list = nullptr;
+  LB_CUDA(cudaMalloc(&S.bucket_count, sizeof(unsigned) * nslabs));
+  LB_CUDA(cudaMalloc(&S.bucket_list, sizeof(int) * (size_t)nslabs * SLAB_BUCKET_CAP));
+  S.bucket_slabs = nslabs;
+  S.bucket_tile = -1;
+  return false;
+}
+
+SlabSpread spread_prepare_slabs(Lattice* L) {
+  SpreadScratch& S = L->spread;
+  if (!ensure_buckets(L) || S.bucket_tile != L->fused_tile) {
+    const TileGrid G = slab_grid(L);
+    LB_CUDA(cudaMemsetAsync(S.bucket_count, 0, sizeof(unsigned) * S.bucket_slabs, L->stream));
+    if (S.pending > 0) {
+      k_bucket_ends<<<(S.pending + 255) / 256, 256, 0, L->stream>>>(
+          S.pending, (const EndRecord<float>*)S.ends, make_dims(L), G, S.bucket_count,
+          S.bucket_list);
+      LB_CHECK_LAUNCH(1);
+    }
+    S.bucket_tile = L->fused_tile;
+  }
   SlabSpread out;
   out.ends = S.ends;
-  out.start = S.slabs.start;
-  out.list = S.slabs.list;
-  out.fixed_scale = fixed_scale_for_pending(L);
+  out.count = S.bucket_count;
+  out.list = S.bucket_list;
+  out.npending = S.pending;
+  out.max_abs_force = S.max_abs_force;
   return out;
 }
 
@@ -1198,15 +1212,26 @@ static void append_ends_t(Swimmers* W, Lattice* L) {
   SpreadScratch& S = L->spread;
   const int nends = 2 * W->n;
   ensure_ends(L, S.pending + nends);
-  if (!S.max_abs_force) {
-    LB_CUDA(cudaMalloc(&S.max_abs_force, sizeof(unsigned)));
-    LB_CUDA(cudaMalloc(&S.fixed_scale, 2 * sizeof(float)));
+  if (!S.max_abs_force) LB_CUDA(cudaMalloc(&S.max_abs_force, sizeof(unsigned)));
+  // reduced-precision lattices list the ends under the step kernel's slabs now
+  constexpr bool BUCKETS = sizeof(T) == 4;
+  bool fill = false;
+  if (BUCKETS) {
+    const bool kept = ensure_buckets(L);
+    if (S.pending == 0) {
+      LB_CUDA(cudaMemsetAsync(S.bucket_count, 0, sizeof(unsigned) * S.bucket_slabs, L->stream));
+      S.bucket_tile = L->fused_tile;
+    } else if (!kept) {
+      S.bucket_tile = -1;
+    }
+    fill = S.bucket_tile == L->fused_tile;
   }
   if (S.pending == 0) LB_CUDA(cudaMemsetAsync(S.max_abs_force, 0, sizeof(unsigned), L->stream));
   if (nends > 0) {
     k_end_records<T><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
         W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L),
-        (EndRecord<T>*)S.ends + S.pending, S.max_abs_force);
+        (EndRecord<T>*)S.ends + S.pending, S.pending, S.max_abs_force, slab_grid(L),
+        fill ? S.bucket_count : nullptr, fill ? S.bucket_list : nullptr);
     LB_CHECK_LAUNCH(1);
   }
   S.pending += nends;
