@@ -16,6 +16,7 @@
 
 #include "lbswim_device.cuh"
 #include "lbswim_internal.h"
+#include "spread_slab.cuh"
 
 namespace lbswim {
 
@@ -293,23 +294,8 @@ __global__ void k_f32_to_f64(const float* __restrict__ src, double* __restrict__
 // used in the collision (lb.cu:286-293) and writes f(t+1), rho, u.  The next
 // plane's loads are issued before the current plane is collided.
 // ---------------------------------------------------------------------------
-constexpr int FUSED_LX = 32;
+constexpr int FUSED_LX = SLAB_LX;
 constexpr int FUSED_RING_THREADS = 96;
-constexpr int SPREAD_CAP = 256;  // ends of one slab held in shared memory
-constexpr int SPREAD_PLANES_PER_END = 8;  // local planes one end can cover (6 at most)
-
-// Local rows / columns of an end's four stencil nodes in a slab's cross-section.
-struct NodeLocal {
-  signed char y[4];
-  signed char z[4];
-};
-
-// What the scatter needs of a pending dipole end, kept in shared memory.
-struct SlabEnd {
-  int ox;          // wrapped x origin of the stencil
-  float F[3];      // force carried by the end
-  float phi[3][4];  // Peskin weights of the 4 nodes per axis
-};
 
 struct FusedArgs {
   const void* f_old;
@@ -320,12 +306,7 @@ struct FusedArgs {
   long long n;
   float rho0;
   Relax<float> k;
-  // pending dipole ends spread by the kernel itself (SPREAD instances)
-  const EndRecord<float>* ends;
-  const unsigned* slab_count;  // [slabs] ends listed per slab (may exceed the capacity)
-  const int* slab_list;        // [slabs][SLAB_BUCKET_CAP]
-  int npending;
-  const unsigned* max_abs_f;   // device: largest |F| component, as float bits
+  SlabEnds spread;  // pending dipole ends spread by the kernel itself (SPREAD instances)
 };
 
 // Post-collision populations wait in shared memory until the output plane can
@@ -348,27 +329,14 @@ __host__ __device__ constexpr int ring_pop_planes() {
   return 5 * (ring_slots<SPREAD>(0) + ring_slots<SPREAD>(1) + ring_slots<SPREAD>(2));
 }
 
-__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
-
-// Shared-memory layout of the SPREAD instances after the ring: fixed-point
-// force sums of one plane as 32-bit halves [3][lo, hi][PLANE], coverage masks [CAP] (u64), ends
-// [CAP], local node rows [CAP], per-plane list offsets [LX + 3], lists.
 template <int TZ, int TY>
-struct SpreadLayout {
-  static constexpr int PLANE = (TY + 2) * (TZ + 2);
-  static constexpr int ring = align16(ring_pop_planes<true>() * PLANE * 4);
-  static constexpr int fq = ring;
-  static constexpr int xmask = align16(fq + 3 * PLANE * 8);
-  static constexpr int ends = align16(xmask + SPREAD_CAP * 8);
-  static constexpr int nodes = align16(ends + SPREAD_CAP * (int)sizeof(SlabEnd));
-  static constexpr int poff = align16(nodes + SPREAD_CAP * (int)sizeof(NodeLocal));
-  static constexpr int plist = align16(poff + (FUSED_LX + 3) * 4);
-  static constexpr int total = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END * 2);
-};
+constexpr int spread_base() {
+  return align16(ring_pop_planes<true>() * (TY + 2) * (TZ + 2) * (int)sizeof(float));
+}
 
 template <int TZ, int TY, bool SPREAD>
 constexpr int fused_smem_bytes() {
-  return SPREAD ? SpreadLayout<TZ, TY>::total
+  return SPREAD ? SpreadLayout<TZ, TY, 1, spread_base<TZ, TY>()>::total
                 : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
 
@@ -416,166 +384,14 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   const int my = ly * HZ + lz;
 
   // ---- this slab's pending dipole ends and the fixed-point force plane ----
-  using SL = SpreadLayout<TZ, TY>;
-  // 64-bit fixed-point sums kept as 32-bit halves [3][lo, hi][PLANE]: 32-bit
-  // shared-memory atomics are native, 64-bit ones are not
-  unsigned* fq = reinterpret_cast<unsigned*>(smraw + SL::fq);
-  // bit kk of xmask[q]: end q covers local plane kk (x = x0 - 1 + kk); FUSED_LX + 2 <= 63;
-  // bit 63: a node of end q appears twice in the cross-section (tiny lattices)
-  unsigned long long* xmask = reinterpret_cast<unsigned long long*>(smraw + SL::xmask);
-  SlabEnd* srec = reinterpret_cast<SlabEnd*>(smraw + SL::ends);
-  NodeLocal* nodes = reinterpret_cast<NodeLocal*>(smraw + SL::nodes);
-  // ends covering each local plane: plist[poff[kk] .. poff[kk + 1]), entries
-  // q | ix << 8 | flags (q indexes srec, ix is the x node on the plane)
-  int* poff = reinterpret_cast<int*>(smraw + SL::poff);
-  unsigned short* plist = reinterpret_cast<unsigned short*>(smraw + SL::plist);
-  constexpr unsigned PL_FOLD = 1u << 10;  // nx < 4: several x nodes fold onto the plane
-  constexpr unsigned PL_DUP = 1u << 11;   // a node appears twice in the cross-section
-  const int fx_exp = SPREAD ? fixed_scale_exp(a.npending, *a.max_abs_f) : 0;
-  const float fx_scale = SPREAD ? exp2_int(fx_exp) : 0.f;
-  const float fx_inv = SPREAD ? exp2_int(-fx_exp) : 0.f;
-  int cnt = 0;
-  long long s0 = 0;
-  bool in_smem = true, overflow = false;
+  SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>()> sp;
+  // the ring threads, which write no output plane, take the first pairs
+  const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
   if (SPREAD) {
     const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    const unsigned c = a.slab_count[slab];
-    // a slab whose bucket overflowed is spread from the whole list of ends
-    overflow = c > (unsigned)SLAB_BUCKET_CAP;
-    cnt = overflow ? a.npending : (int)c;
-    s0 = (long long)slab * SLAB_BUCKET_CAP;
-    in_smem = !overflow && cnt <= SPREAD_CAP;
-    if (in_smem) {
-      for (int q = tid; q < cnt; q += blockDim.x) {
-        const EndRecord<float>& g = a.ends[a.slab_list[s0 + q]];
-        SlabEnd e;
-        e.ox = g.o[0];
-        for (int c = 0; c < 3; ++c) {
-          e.F[c] = g.F[c];
-          for (int j = 0; j < 4; ++j) e.phi[c][j] = g.phi[c][j];
-        }
-        unsigned long long m = 0ull;
-        float w;
-        for (int kk = 0; kk < ex + 2; ++kk)
-          if (cover_weight(wrap_once(x0 - 1 + kk, nx), e.ox, nx, e.phi[0], w)) m |= 1ull << kk;
-        // local row / column of each stencil node in the halo-inclusive
-        // cross-section (-1: outside)
-        NodeLocal nl;
-        for (int j = 0; j < 4; ++j) {
-          const int ly2 = wrap_any(wrap_any(g.o[1] + j, ny) - y0 + 1, ny);
-          const int lz2 = wrap_any(wrap_any(g.o[2] + j, nz) - z0 + 1, nz);
-          nl.y[j] = (signed char)(ly2 <= ey + 1 ? ly2 : -1);
-          nl.z[j] = (signed char)(lz2 <= ez + 1 ? lz2 : -1);
-          if (ly2 + ny <= ey + 1 || lz2 + nz <= ez + 1) m |= 1ull << 63;
-        }
-        srec[q] = e;
-        nodes[q] = nl;
-        xmask[q] = m;
-      }
-    }
-    for (int i = tid; i < 3 * 2 * PLANE; i += blockDim.x) fq[i] = 0u;
-    __syncthreads();
-    if (in_smem) {
-      // per-plane lists in increasing end position: count, offsets, fill
-      const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-      for (int kk = warp; kk < ex + 2; kk += nwarps) {
-        int c = 0;
-        for (int base = 0; base < cnt; base += 32) {
-          const int q = base + lane;
-          c += __popc(__ballot_sync(0xffffffffu, q < cnt && ((xmask[q] >> kk) & 1ull)));
-        }
-        if (lane == 0) poff[kk + 1] = c;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        poff[0] = 0;
-        for (int kk = 0; kk < ex + 2; ++kk) poff[kk + 1] += poff[kk];
-      }
-      __syncthreads();
-      for (int kk = warp; kk < ex + 2; kk += nwarps) {
-        int at = poff[kk];
-        for (int base = 0; base < cnt; base += 32) {
-          const int q = base + lane;
-          const bool cov = q < cnt && ((xmask[q] >> kk) & 1ull);
-          const unsigned m = __ballot_sync(0xffffffffu, cov);
-          if (cov) {
-            int ix = wrap_once(x0 - 1 + kk, nx) - srec[q].ox;
-            if (ix < 0) ix += nx;
-            const unsigned ent = (unsigned)q | (nx >= 4 ? (unsigned)ix << 8 : PL_FOLD) |
-                                 ((xmask[q] >> 63) ? PL_DUP : 0u);
-            plist[at + __popc(m & ((1u << lane) - 1u))] = (unsigned short)ent;
-          }
-          at += __popc(m);
-        }
-      }
-      __syncthreads();
-    }
-  }
-  // Add every end-node contribution of local plane kk into fq: the pairs
-  // (end, (jy, jz) node) are shared among all threads of the CTA.
-  auto scatter_plane = [&](int kk) {
-    const int gx = wrap_once(x0 - 1 + kk, nx);
-    // exact 64-bit addition: the low half's carry goes into the high half
-    auto add1 = [&](unsigned* lo, long long q) {
-      const unsigned l = (unsigned)q;
-      const unsigned old = atomicAdd(lo, l);
-      const int h = (int)(q >> 32) + (old + l < old ? 1 : 0);
-      if (h != 0) atomicAdd(reinterpret_cast<int*>(lo + PLANE), h);
-    };
-    auto add3 = [&](int at, long long q0, long long q1, long long q2) {
-      add1(fq + at, q0);
-      add1(fq + 2 * PLANE + at, q1);
-      add1(fq + 4 * PLANE + at, q2);
-    };
-    if (in_smem) {
-      // (end, node) pairs of the ends covering this plane, on contiguous
-      // threads; the ring threads, which write no output plane, go first
-      const int p0 = poff[kk], np = poff[kk + 1] - p0;
-      const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
-      for (int t = rt; t < np * 16; t += blockDim.x) {
-        const unsigned ent = plist[p0 + (t >> 4)];
-        const int q = (int)(ent & 0xffu);
-        const int jy = (t >> 2) & 3, jz = t & 3;
-        const int ly2 = nodes[q].y[jy], lz2 = nodes[q].z[jz];
-        if ((ly2 | lz2) < 0) continue;  // node outside this cross-section
-        const SlabEnd& e = srec[q];
-        float wx;
-        if (ent & PL_FOLD)
-          cover_weight(gx, e.ox, nx, e.phi[0], wx);
-        else
-          wx = e.phi[0][(ent >> 8) & 3u];
-        const float py = e.phi[1][jy], pz = e.phi[2][jz];
-        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
-        if (!(ent & PL_DUP)) {
-          add3(ly2 * HZ + lz2, q0, q1, q2);
-        } else {
-          // tiny lattice: a node can appear at several places of the cross-section
-          for (int a2 = ly2; a2 <= ey + 1; a2 += ny)
-            for (int b2 = lz2; b2 <= ez + 1; b2 += nz) add3(a2 * HZ + b2, q0, q1, q2);
-        }
-      }
-    } else {
-      // more ends than shared memory holds: every end, records from global memory
-      for (int t = tid; t < cnt * 16; t += blockDim.x) {
-        const EndRecord<float>& e = a.ends[overflow ? (t >> 4) : a.slab_list[s0 + (t >> 4)]];
-        float wx;
-        if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
-        const int jy = (t >> 2) & 3, jz = t & 3;
-        const float py = e.phi[1][jy], pz = e.phi[2][jz];
-        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
-        const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
-        for (int ly2 = wrap_any(yg - y0 + 1, ny); ly2 <= ey + 1; ly2 += ny)
-          for (int lz2 = wrap_any(zg - z0 + 1, nz); lz2 <= ez + 1; lz2 += nz)
-            add3(ly2 * HZ + lz2, q0, q1, q2);
-      }
-    }
-  };
-  if (SPREAD) {
-    scatter_plane(0);
+    sp.bind(smraw, a.spread, slab, nx, ny, nz, x0, y0, z0, ex, ey, ez);
+    sp.prologue(tid, blockDim.x);
+    sp.scatter(0, rt, blockDim.x);
     __syncthreads();
   }
 
@@ -602,15 +418,9 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     for (int i = 0; i < 18; ++i) cur[i] = pre[i];
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
     if (SPREAD && active) {
-      // force = base + spread (k_force_tile writes the same bits)
-      unsigned* f0 = fq + my;
+      // force = base + spread (k_force_slab writes the same bits)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const long long q = (long long)(((unsigned long long)f0[(2 * c + 1) * PLANE] << 32) |
-                                        f0[2 * c * PLANE]);
-        cur[15 + c] += fx_value(q, fx_inv);
-        f0[2 * c * PLANE] = f0[(2 * c + 1) * PLANE] = 0u;  // ready for plane k + 1
-      }
+      for (int c = 0; c < 3; ++c) cur[15 + c] += sp.take(my, c);
     }
     // ring slots: plane k is written to A[k % NA], B[k % NB], C[k % NC]
     const int wa_slot = SPREAD ? k3 : (k & 3);
@@ -631,7 +441,7 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
       }
     }
     __syncthreads();
-    if (SPREAD && k + 1 < ex + 2) scatter_plane(k + 1);
+    if (SPREAD && k + 1 < ex + 2) sp.scatter(k + 1, rt, blockDim.x);
     if (k >= 2 && interior) {
       // output plane x = x0 + k - 2 pulls A of plane x-1, B of x, C of x+1
       const int ra_slot = SPREAD ? (k3 == 2 ? 0 : k3 + 1) : ((k - 2) & 3);
@@ -665,6 +475,68 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     Fp2 = cur[17];
     k3 = k3 == 2 ? 0 : k3 + 1;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Dense force of a reduced-precision lattice: base + the spread of the pending
+// ends, slab by slab and plane by plane with the step kernel's spreading, so
+// the bits are those the step kernel uses.  One thread per (y, z) site of the
+// slab's cross-section writes the three components of its site on each plane.
+// ---------------------------------------------------------------------------
+template <int TZ, int TY>
+__global__ void __launch_bounds__(TY * TZ) k_force_slab(SlabEnds se, float* __restrict__ force,
+                                                         int nx, int ny, int nz, long long N,
+                                                         int accumulate) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int tid = threadIdx.x;
+  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * SLAB_LX;
+  const int ez = min(TZ, nz - z0), ey = min(TY, ny - y0), ex = min(SLAB_LX, nx - x0);
+  const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  SlabSpreader<TZ, TY, 0, 0> sp;
+  sp.bind(smraw, se, slab, nx, ny, nz, x0, y0, z0, ex, ey, ez);
+  sp.prologue(tid, blockDim.x);
+  const int ly = tid / TZ, lz = tid % TZ;
+  const bool valid = ly < ey && lz < ez;
+  const int my = ly * TZ + lz;
+  const long long yz = (long long)(y0 + ly) * nz + (z0 + lz), nynz = (long long)ny * nz;
+  for (int kk = 0; kk < ex; ++kk) {
+    sp.scatter(kk, tid, blockDim.x);
+    __syncthreads();
+    if (valid) {
+      const long long s = (long long)(x0 + kk) * nynz + yz;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float v = sp.take(my, c);
+        force[c * N + s] = accumulate ? force[c * N + s] + v : v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int TZ, int TY>
+static void force_slab_launch(Lattice* L, const SlabSpread& sp) {
+  constexpr int smem = SpreadLayout<TZ, TY, 0, 0>::total;
+  static bool configured = false;
+  if (!configured) {
+    LB_CUDA(cudaFuncSetAttribute(k_force_slab<TZ, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+    configured = true;
+  }
+  dim3 grid((L->size[2] + TZ - 1) / TZ, (L->size[1] + TY - 1) / TY,
+            (L->size[0] + SLAB_LX - 1) / SLAB_LX);
+  k_force_slab<TZ, TY><<<grid, TY * TZ, smem, L->stream>>>(
+      SlabEnds{(const EndRecord<float>*)sp.ends, sp.count, sp.list, sp.npending, sp.max_abs_force},
+      (float*)L->force, L->size[0], L->size[1], L->size[2], L->n, L->force_zero_pending ? 0 : 1);
+  LB_CHECK_LAUNCH(1);
+}
+
+void lattice_force_from_slabs(Lattice* L) {
+  const SlabSpread sp = spread_prepare_slabs(L);
+  if (L->fused_tile == 1)
+    force_slab_launch<16, 16>(L, sp);
+  else
+    force_slab_launch<32, 8>(L, sp);
 }
 
 // ---------------------------------------------------------------------------
@@ -789,15 +661,16 @@ static void launch_fused(Lattice* L, const FusedArgs& a) {
   LB_CHECK_LAUNCH(1);
 }
 
+// Pending dipole ends are spread by the step kernel itself (true), or first
+// into the dense force by k_force_slab (false); both give the same force bits.
+constexpr bool STEP_SPREADS_IN_KERNEL = true;
+
 template <class S, int TZ, int TY>
 static void fused_step_tile(Lattice* L, FusedArgs& a) {
-  if (L->spread.pending > 0) {
+  if (L->spread.pending > 0 && STEP_SPREADS_IN_KERNEL) {
     const SlabSpread sp = spread_prepare_slabs(L);
-    a.ends = (const EndRecord<float>*)sp.ends;
-    a.slab_count = sp.count;
-    a.slab_list = sp.list;
-    a.npending = sp.npending;
-    a.max_abs_f = sp.max_abs_force;
+    a.spread = SlabEnds{(const EndRecord<float>*)sp.ends, sp.count, sp.list, sp.npending,
+                        sp.max_abs_force};
     launch_fused<S, TZ, TY, true>(L, a);
   } else {
     launch_fused<S, TZ, TY, false>(L, a);
@@ -812,6 +685,7 @@ void fused_slab_shape(const Lattice* L, int T[3]) {
 
 template <class S>
 static void fused_step_t(Lattice* L) {
+  if (!STEP_SPREADS_IN_KERNEL && L->spread.pending > 0) spread_materialise(L);
   FusedArgs a{};
   a.f_old = L->f[L->cur];
   a.f_new = L->f[L->cur ^ 1];

@@ -190,6 +190,9 @@ SlabSpread spread_prepare_slabs(Lattice* L);
 // Slab shape of the fused step kernel for a lattice: x planes per slab, rows,
 // columns (lattice.cu).
 void fused_slab_shape(const Lattice* L, int T[3]);
+// Dense force (base + spread of the pending ends) of a reduced-precision
+// lattice, bit for bit the force the step kernel spreads (lattice.cu).
+void lattice_force_from_slabs(Lattice* L);
 void spread_free(SpreadScratch& S);
 
 // particles.cu

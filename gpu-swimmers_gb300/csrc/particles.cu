@@ -1149,10 +1149,14 @@ static void materialise_t(Lattice* L) {
 
 void spread_materialise(Lattice* L) {
   if (L->spread.pending > 0) {
-    if (L->precision == LBSWIM_F64)
+    if (L->precision == LBSWIM_F64) {
       materialise_t<double>(L);
-    else
-      materialise_t<float>(L);
+    } else {
+      lattice_force_from_slabs(L);
+      L->spread.pending = 0;
+      L->spread.stepped = false;
+      L->force_zero_pending = false;
+    }
   } else if (L->force_zero_pending) {
     lattice_zero_force_now(L);
   }
