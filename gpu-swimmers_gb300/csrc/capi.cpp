@@ -200,7 +200,8 @@ int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out) {
 int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags) {
   API_BEGIN
   check_lattice(lat);
-  REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP)) == 0,
+  REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP |
+                      LBSWIM_COMPAT_EXACT_F64)) == 0,
           "unknown compat flag");
   LAT(lat)->compat = flags;
   API_END

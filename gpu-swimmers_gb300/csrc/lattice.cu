@@ -639,7 +639,12 @@ static void init_from_hydro_t(Lattice* L) {
 
 void lattice_init_from_hydro(Lattice* L) {
   switch (L->precision) {
-    case LBSWIM_F64: init_from_hydro_t<double>(L); break;
+    case LBSWIM_F64:
+      if (L->compat & LBSWIM_COMPAT_EXACT_F64)
+        exact_init_from_hydro_f64(L);
+      else
+        init_from_hydro_t<double>(L);
+      break;
     case LBSWIM_F32: init_from_hydro_t<float>(L); break;
     case LBSWIM_BF16: init_from_hydro_t<__nv_bfloat16>(L); break;
     default: init_from_hydro_t<__half>(L); break;
@@ -750,7 +755,9 @@ void lattice_step(Lattice* L) {
     ev = timing_pair(L);
     LB_CUDA(cudaEventRecord(ev.first, L->stream));
   }
-  if (L->precision == LBSWIM_F64) {
+  if (L->precision == LBSWIM_F64 && (L->compat & LBSWIM_COMPAT_EXACT_F64)) {
+    exact_step_f64(L);
+  } else if (L->precision == LBSWIM_F64) {
     dim3 grid((nz + 31) / 32, (ny + 7) / 8, nx);
     k_step_push_f64<<<grid, dim3(32, 8), 0, L->stream>>>(
         (const double*)L->f[L->cur], L->force_zero_pending ? nullptr : (const double*)L->force,
@@ -803,7 +810,12 @@ void lattice_calc_hydro(Lattice* L) {
   lattice_materialise_force(L);
   lattice_wait_readers(L, L->precision == LBSWIM_F64 ? nullptr : (const void*)L->hydro);
   switch (L->precision) {
-    case LBSWIM_F64: calc_hydro_t<double>(L); break;
+    case LBSWIM_F64:
+      if (L->compat & LBSWIM_COMPAT_EXACT_F64)
+        exact_calc_hydro_f64(L);
+      else
+        calc_hydro_t<double>(L);
+      break;
     case LBSWIM_F32: calc_hydro_t<float>(L); break;
     case LBSWIM_BF16: calc_hydro_t<__nv_bfloat16>(L); break;
     default: calc_hydro_t<__half>(L); break;

@@ -216,6 +216,25 @@ __device__ __forceinline__ T peskin_delta(T x) {
   }
   return T(0.125) * phi;
 }
+// FP64: the reference's operations in its order, each rounded on its own (no
+// fused multiply-add), so that FP64 lattices can reproduce the oracle bit for bit.
+template <>
+__device__ __forceinline__ double peskin_delta<double>(double x) {
+  const double ax = fabs(x);
+  double root = __dmul_rn(__dmul_rn(-4.0, x), x);
+  double phi = __dmul_rn(-2.0, ax);
+  if (ax >= 2.0) return 0.0;
+  if (ax >= 1.0) {
+    root = __dadd_rn(root, __dsub_rn(__dmul_rn(12.0, ax), 7.0));
+    phi = __dadd_rn(phi, 5.0);
+    phi = __dsub_rn(phi, __dsqrt_rn(root));
+  } else {
+    root = __dadd_rn(root, __dadd_rn(__dmul_rn(4.0, ax), 1.0));
+    phi = __dadd_rn(phi, 3.0);
+    phi = __dadd_rn(phi, __dsqrt_rn(root));
+  }
+  return __dmul_rn(0.125, phi);
+}
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------------
 __device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -254,19 +273,96 @@ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
   const uint64_t m = ((uint64_t)a << 21) | (uint64_t)(b >> 11);
   return (double)(m + 1u) * 0x1.0p-53;
 }
+// log x for a normal x > 0, as a fixed sequence of correctly rounded FP64
+// operations (the oracle performs the same ones): x = m 2^e with m in
+// [sqrt(1/2), sqrt(2)], log m = 2 atanh s, s = (m - 1)/(m + 1), the atanh
+// series to the s^27 term in Horner form, ln 2 split into a 40-bit head
+// (e ln2_hi exact) and a tail.
+__device__ __forceinline__ double det_log(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  b = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;  // m in [1, 2)
+  double m = __longlong_as_double((long long)b);
+  if (m > 1.4142135623730951) {
+    m = __dmul_rn(m, 0.5);
+    e += 1;
+  }
+  const double s = __ddiv_rn(__dsub_rn(m, 1.0), __dadd_rn(m, 1.0));
+  const double z = __dmul_rn(s, s);
+  double p = 0.037037037037037035;  // 1/27 ... 1/3
+  p = __dadd_rn(__dmul_rn(p, z), 0.040000000000000001);
+  p = __dadd_rn(__dmul_rn(p, z), 0.043478260869565216);
+  p = __dadd_rn(__dmul_rn(p, z), 0.047619047619047616);
+  p = __dadd_rn(__dmul_rn(p, z), 0.052631578947368418);
+  p = __dadd_rn(__dmul_rn(p, z), 0.058823529411764705);
+  p = __dadd_rn(__dmul_rn(p, z), 0.066666666666666666);
+  p = __dadd_rn(__dmul_rn(p, z), 0.076923076923076927);
+  p = __dadd_rn(__dmul_rn(p, z), 0.090909090909090912);
+  p = __dadd_rn(__dmul_rn(p, z), 0.1111111111111111);
+  p = __dadd_rn(__dmul_rn(p, z), 0.14285714285714285);
+  p = __dadd_rn(__dmul_rn(p, z), 0.20000000000000001);
+  p = __dadd_rn(__dmul_rn(p, z), 0.33333333333333331);
+  const double t = __dmul_rn(2.0, s);
+  const double lm = __dadd_rn(t, __dmul_rn(t, __dmul_rn(z, p)));
+  const double de = (double)e;
+  return __dadd_rn(__dmul_rn(de, 0.69314718055920821),
+                   __dadd_rn(__dmul_rn(de, 7.3710025651677989e-13), lm));
+}
+
+// sin(2 pi u), cos(2 pi u) for 0 <= u <= 1 a multiple of 2^-53 (the oracle
+// performs the same operations): u = k/8 + f, |f| <= 1/16, theta = 2 pi f,
+// Taylor series to theta^17 / theta^18, then the angle sum with sin, cos of
+// k pi / 4.
+__device__ __forceinline__ void det_sincos2pi(double u, double& sn, double& cs) {
+  const double k = floor(__dadd_rn(__dmul_rn(u, 8.0), 0.5));
+  const double f = __dsub_rn(u, __dmul_rn(k, 0.125));
+  const double th = __dmul_rn(f, 6.2831853071795862);
+  const double z = __dmul_rn(th, th);
+  double ps = 2.8114572543455206e-15;
+  ps = __dadd_rn(__dmul_rn(ps, z), -7.6471637318198164e-13);
+  ps = __dadd_rn(__dmul_rn(ps, z), 1.6059043836821613e-10);
+  ps = __dadd_rn(__dmul_rn(ps, z), -2.505210838544172e-08);
+  ps = __dadd_rn(__dmul_rn(ps, z), 2.7557319223985893e-06);
+  ps = __dadd_rn(__dmul_rn(ps, z), -0.00019841269841269841);
+  ps = __dadd_rn(__dmul_rn(ps, z), 0.0083333333333333332);
+  ps = __dadd_rn(__dmul_rn(ps, z), -0.16666666666666666);
+  double pc = -1.5619206968586225e-16;
+  pc = __dadd_rn(__dmul_rn(pc, z), 4.7794773323873853e-14);
+  pc = __dadd_rn(__dmul_rn(pc, z), -1.1470745597729725e-11);
+  pc = __dadd_rn(__dmul_rn(pc, z), 2.08767569878681e-09);
+  pc = __dadd_rn(__dmul_rn(pc, z), -2.7557319223985888e-07);
+  pc = __dadd_rn(__dmul_rn(pc, z), 2.4801587301587302e-05);
+  pc = __dadd_rn(__dmul_rn(pc, z), -0.0013888888888888889);
+  pc = __dadd_rn(__dmul_rn(pc, z), 0.041666666666666664);
+  pc = __dadd_rn(__dmul_rn(pc, z), -0.5);
+  const double s = __dadd_rn(th, __dmul_rn(th, __dmul_rn(z, ps)));
+  const double c = __dadd_rn(1.0, __dmul_rn(z, pc));
+  const int ki = ((int)k) & 7;
+  const double r = 0.70710678118654757;
+  double sa = (ki == 0 || ki == 4) ? 0.0 : ((ki == 2) ? 1.0 : ((ki == 6) ? -1.0 : (ki < 4 ? 1.0 : -1.0)));
+  double ca = (ki == 2 || ki == 6) ? 0.0 : ((ki == 0) ? 1.0 : ((ki == 4) ? -1.0 : ((ki == 1 || ki == 7) ? 1.0 : -1.0)));
+  if (ki & 1) {
+    sa = __dmul_rn(sa, r);
+    ca = __dmul_rn(ca, r);
+  }
+  sn = __dadd_rn(__dmul_rn(sa, c), __dmul_rn(ca, s));
+  cs = __dsub_rn(__dmul_rn(ca, c), __dmul_rn(sa, s));
+}
+
+// Three normal deviates of a tumble (Box-Muller on 53-bit uniforms).
 __device__ __forceinline__ void rng_normal3(uint64_t seed, uint32_t swimmer, uint64_t step,
                                             double g[3]) {
   uint32_t a[4], b[4];
   rng_block(seed, swimmer, step, 1u, a);
   rng_block(seed, swimmer, step, 2u, b);
-  const double twopi = 6.283185307179586;
-  const double r1 = sqrt(-2.0 * log(u53(a[0], a[1])));
-  const double r2 = sqrt(-2.0 * log(u53(b[0], b[1])));
-  const double t1 = twopi * u53(a[2], a[3]);
-  const double t2 = twopi * u53(b[2], b[3]);
-  g[0] = r1 * cos(t1);
-  g[1] = r1 * sin(t1);
-  g[2] = r2 * cos(t2);
+  const double r1 = __dsqrt_rn(__dmul_rn(-2.0, det_log(u53(a[0], a[1]))));
+  const double r2 = __dsqrt_rn(__dmul_rn(-2.0, det_log(u53(b[0], b[1]))));
+  double s2, c2, s4, c4;
+  det_sincos2pi(u53(a[2], a[3]), s2, c2);
+  det_sincos2pi(u53(b[2], b[3]), s4, c4);
+  g[0] = __dmul_rn(r1, c2);
+  g[1] = __dmul_rn(r1, s2);
+  g[2] = __dmul_rn(r2, c4);
 }
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -411,7 +507,7 @@ __device__ __forceinline__ bool cover_weight4(int x, int o, int n, const float4&
 // plane.  Every FP32 kernel that spreads uses this one expression, so the
 // step kernel's own spreading and the materialised force agree bit for bit.
 __device__ __forceinline__ double end_contrib(double wx, double wy, double wz, double F) {
-  return (wx * wy * wz) * F;
+  return __dmul_rn(__dmul_rn(__dmul_rn(wx, wy), wz), F);
 }
 __device__ __forceinline__ float end_contrib_f(float wy, float wz, float wxF) {
   return (wy * wz) * wxF;

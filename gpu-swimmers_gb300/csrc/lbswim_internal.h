@@ -184,6 +184,12 @@ void lattice_zero_force(Lattice* L);
 void lattice_wait_readers(Lattice* L, const void* buf);
 inline void lattice_join(Lattice* L) { lattice_wait_readers(L, nullptr); }
 
+// exact_f64.cu: FP64 lattice ops in the reference's operation order
+// (LBSWIM_COMPAT_EXACT_F64)
+void exact_step_f64(Lattice* L);
+void exact_calc_hydro_f64(Lattice* L);
+void exact_init_from_hydro_f64(Lattice* L);
+
 // particles.cu: force spreading state
 void spread_materialise(Lattice* L);
 SlabSpread spread_prepare_slabs(Lattice* L);

@@ -30,6 +30,16 @@ struct Dims {
   long long N;
 };
 
+// acc + a b: FP64 rounds the product and the sum on their own (the oracle's
+// order, bit for bit); FP32 lets the compiler fuse them.
+template <class T>
+__device__ __forceinline__ T add_prod(T acc, T a, T b) {
+  if constexpr (sizeof(T) == 8)
+    return __dadd_rn(acc, __dmul_rn(a, b));
+  else
+    return acc + a * b;
+}
+
 template <class T>
 __device__ __forceinline__ void stencil_setup(const Dims& D, const double r[3], int o[3],
                                               T phi[3][4]) {
@@ -53,7 +63,7 @@ __global__ void k_spread_bin(int nsw, const double* __restrict__ r, const double
   double rr[3], F[3];
   for (int a = 0; a < 3; ++a) {
     const double na = nv[nsw * a + i];
-    rr[a] = head ? r[nsw * a + i] : r[nsw * a + i] - na * l;
+    rr[a] = head ? r[nsw * a + i] : __dsub_rn(r[nsw * a + i], __dmul_rn(na, l));
     F[a] = -P * na;
     if (head) F[a] *= -1.0;
   }
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(REC_THREADS) k_end_records(
     double rr[3], F[3];
     for (int a = 0; a < 3; ++a) {
       const double na = nv[nsw * a + i];
-      rr[a] = head ? r[nsw * a + i] : r[nsw * a + i] - na * l;
+      rr[a] = head ? r[nsw * a + i] : __dsub_rn(r[nsw * a + i], __dmul_rn(na, l));
       F[a] = -P * na;
       if (head) F[a] *= -1.0;
     }
@@ -473,7 +483,15 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
   for (int row = warp; row < FT_X * FT_Y; row += FT_THREADS / 32) {
     const int x = kx * FT_X + (row >> 3), y = ky * FT_Y + (row & 7);
     if (x >= D.n[0] || y >= D.n[1]) continue;
+    const long long s = (long long)x * D.n[1] * D.n[2] + (long long)y * D.n[2] + z;
+    // FP64 sums start from the base force and add the ends in end order, as
+    // the oracle's serial spreading does
     T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+    if (!FIXED && accumulate && zval) {
+      acc0 = force[s];
+      acc1 = force[D.N + s];
+      acc2 = force[2 * D.N + s];
+    }
     long long q0 = 0, q1 = 0, q2 = 0;
     bool hit = false;
     for (int base = 0; base < cnt; base += 32) {
@@ -507,15 +525,25 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
             }
           }
         } else {
-          cover_weight(y, e.o[1], D.n[1], e.phi[1], wy);
-          acc0 += end_contrib(wx, wy, wz, e.F[0]);
-          acc1 += end_contrib(wx, wy, wz, e.F[1]);
-          acc2 += end_contrib(wx, wy, wz, e.F[2]);
+          // node by node in (i, j, k) order, as AccumulateDeltaForce adds them
+          // (several nodes land on one site when an axis is shorter than 4)
+          (void)wy;
+          for (int i = 0; i < 4; ++i) {
+            if (wrap_any(e.o[0] + i, D.n[0]) != x) continue;
+            for (int j = 0; j < 4; ++j) {
+              if (wrap_any(e.o[1] + j, D.n[1]) != y) continue;
+              for (int k = 0; k < 4; ++k) {
+                if (wrap_any(e.o[2] + k, D.n[2]) != z) continue;
+                acc0 = __dadd_rn(acc0, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[0]));
+                acc1 = __dadd_rn(acc1, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[1]));
+                acc2 = __dadd_rn(acc2, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[2]));
+              }
+            }
+          }
         }
       }
     }
     if (!zval) continue;
-    const long long s = (long long)x * D.n[1] * D.n[2] + (long long)y * D.n[2] + z;
     if constexpr (FIXED) {
       // base + spread, the value the step kernel forms
       const T b0 = accumulate ? force[s] : T(0), b1 = accumulate ? force[D.N + s] : T(0),
@@ -523,14 +551,10 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
       force[s] = b0 + fx_value(q0, fx_inv);
       force[D.N + s] = b1 + fx_value(q1, fx_inv);
       force[2 * D.N + s] = b2 + fx_value(q2, fx_inv);
-    } else if (!accumulate) {
+    } else if (!accumulate || hit) {
       force[s] = acc0;
       force[D.N + s] = acc1;
       force[2 * D.N + s] = acc2;
-    } else if (hit) {
-      force[s] += acc0;
-      force[D.N + s] += acc1;
-      force[2 * D.N + s] += acc2;
     }
   }
 }
@@ -590,9 +614,9 @@ __device__ __forceinline__ void interp_velocity(const double* __restrict__ u, co
       for (int k = 0; k < 4; ++k) {
         const T d3 = pij * phi[2][k];
         const long long s = row + idx[2][k];
-        v[0] += d3 * (T)u[s];
-        v[1] += d3 * (T)u[D.N + s];
-        v[2] += d3 * (T)u[2 * D.N + s];
+        v[0] = add_prod(v[0], d3, (T)u[s]);
+        v[1] = add_prod(v[1], d3, (T)u[D.N + s]);
+        v[2] = add_prod(v[2], d3, (T)u[2 * D.N + s]);
       }
     }
 }
@@ -639,9 +663,9 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
   interp_velocity<T>(u, D, r, v);
   double rMinus[3];
   for (int d = 0; d < 3; ++d) {
-    double rDot = c.mobility * c.P * n0[d];
-    if (!c.translational_advection_off) rDot += (double)v[d];
-    rMinus[d] = r[d] - n0[d] * c.l;
+    double rDot = __dmul_rn(__dmul_rn(c.mobility, c.P), n0[d]);
+    if (!c.translational_advection_off) rDot = __dadd_rn(rDot, (double)v[d]);
+    rMinus[d] = __dsub_rn(r[d], __dmul_rn(n0[d], c.l));
     swv[nsw * d + i] = rDot;
     swr[nsw * d + i] = wrap_position<T>(r[d] + rDot, D.n[d]);
   }
@@ -656,7 +680,8 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
   } else {
     return;  // orientation unchanged
   }
-  const double norm = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+  const double norm = __dsqrt_rn(
+      __dadd_rn(__dadd_rn(__dmul_rn(nn[0], nn[0]), __dmul_rn(nn[1], nn[1])), __dmul_rn(nn[2], nn[2])));
   for (int d = 0; d < 3; ++d) swn[nsw * d + i] = nn[d] / norm;
 }
 

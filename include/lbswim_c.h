@@ -70,6 +70,13 @@ extern "C" {
 #define LBSWIM_COMPAT_INIT_SXZ 1
 /* Synchronise the device at the end of every Step, as lb.cu:239 does. */
 #define LBSWIM_COMPAT_SYNC_STEP 2
+/* FP64 lattices only: Step, CalcHydro and InitFromHydro use the reference's
+ * dense 15x15 transforms in its operation order (lb.cu:72-218, 250-295,
+ * 314-371), every operation rounded on its own, so that results are bit for
+ * bit those of the reference's host build (about 3x the FP64 work of the
+ * default butterfly transform).  The particle kernels of FP64 lattices always
+ * follow the reference's operation order. */
+#define LBSWIM_COMPAT_EXACT_F64 4
 
 typedef struct lbswim_lattice lbswim_lattice;
 typedef struct lbswim_swimmers lbswim_swimmers;

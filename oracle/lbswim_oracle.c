@@ -193,18 +193,86 @@ static double u53(uint32_t a, uint32_t b) {
   return (double)(m + 1u) * 0x1.0p-53;
 }
 
+/* log x (0 < x, x normal) as a fixed sequence of IEEE double operations, so
+ * that the oracle and the GPU form identical normals (no libm call, whose last
+ * bits differ between libraries).  x = m 2^e with m in [sqrt(1/2), sqrt(2)];
+ * log m = 2 atanh s with s = (m - 1)/(m + 1), |s| <= 0.1716, and
+ * atanh s = s + s^3/3 + s^5/5 + ... to the s^27 term (Horner in z = s^2);
+ * ln 2 is split into a 40-bit head and a tail so e ln2_hi is exact.  The same
+ * operations, in the same order, are in the device code. */
+static const double DET_LN2_HI = 0.69314718055920821, DET_LN2_LO = 7.3710025651677989e-13;
+static const double DET_ATANH[13] = {
+    0.33333333333333331, 0.20000000000000001, 0.14285714285714285, 0.1111111111111111,
+    0.090909090909090912, 0.076923076923076927, 0.066666666666666666, 0.058823529411764705,
+    0.052631578947368418, 0.047619047619047616, 0.043478260869565216, 0.040000000000000001,
+    0.037037037037037035};
+double orc_det_log(double x) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  b = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull; /* m in [1, 2) */
+  double m;
+  memcpy(&m, &b, 8);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double z = s * s;
+  double p = DET_ATANH[12];
+  for (int k = 11; k >= 0; --k) p = p * z + DET_ATANH[k];
+  const double t = 2.0 * s;
+  const double lm = t + t * (z * p);
+  const double de = (double)e;
+  return de * DET_LN2_HI + (de * DET_LN2_LO + lm);
+}
+
+/* sin(2 pi u), cos(2 pi u) for 0 <= u <= 1 a multiple of 2^-53: u = k/8 + f
+ * with |f| <= 1/16 (exact), theta = 2 pi f, Taylor series of sin and cos to
+ * the theta^17 and theta^18 terms, then the angle sum with sin, cos of
+ * k pi / 4 in {0, +-1, +-sqrt(1/2)}. */
+static const double DET_SIN[8] = {-0.16666666666666666, 0.0083333333333333332,
+                                  -0.00019841269841269841, 2.7557319223985893e-06,
+                                  -2.505210838544172e-08, 1.6059043836821613e-10,
+                                  -7.6471637318198164e-13, 2.8114572543455206e-15};
+static const double DET_COS[9] = {-0.5, 0.041666666666666664, -0.0013888888888888889,
+                                  2.4801587301587302e-05, -2.7557319223985888e-07,
+                                  2.08767569878681e-09, -1.1470745597729725e-11,
+                                  4.7794773323873853e-14, -1.5619206968586225e-16};
+void orc_det_sincos2pi(double u, double* sn, double* cs) {
+  const double k = floor(u * 8.0 + 0.5);
+  const double f = u - k * 0.125;
+  const double th = f * 6.2831853071795862;
+  const double z = th * th;
+  double ps = DET_SIN[7];
+  for (int i = 6; i >= 0; --i) ps = ps * z + DET_SIN[i];
+  double pc = DET_COS[8];
+  for (int i = 7; i >= 0; --i) pc = pc * z + DET_COS[i];
+  const double s = th + th * (z * ps);
+  const double c = 1.0 + z * pc;
+  const double r = 0.70710678118654757;
+  static const double SA[8] = {0., 1., 1., 1., 0., -1., -1., -1.};
+  static const double CA[8] = {1., 1., 0., -1., -1., -1., 0., 1.};
+  const int ki = ((int)k) & 7;
+  const double sa = (ki & 1) ? SA[ki] * r : SA[ki], ca = (ki & 1) ? CA[ki] * r : CA[ki];
+  *sn = sa * c + ca * s;
+  *cs = ca * c - sa * s;
+}
+
 void orc_rng_normal3(uint64_t seed, uint32_t swimmer, uint64_t step, double out[3]) {
   uint32_t a[4], b[4];
   rng_block(seed, swimmer, step, 1u, a);
   rng_block(seed, swimmer, step, 2u, b);
-  const double twopi = 6.283185307179586;
   const double u1 = u53(a[0], a[1]), u2 = u53(a[2], a[3]);
   const double u3 = u53(b[0], b[1]), u4 = u53(b[2], b[3]);
-  const double r1 = sqrt(-2.0 * log(u1));
-  const double r2 = sqrt(-2.0 * log(u3));
-  out[0] = r1 * cos(twopi * u2);
-  out[1] = r1 * sin(twopi * u2);
-  out[2] = r2 * cos(twopi * u4);
+  const double r1 = sqrt(-2.0 * orc_det_log(u1));
+  const double r2 = sqrt(-2.0 * orc_det_log(u3));
+  double s2, c2, s4, c4;
+  orc_det_sincos2pi(u2, &s2, &c2);
+  orc_det_sincos2pi(u4, &s4, &c4);
+  out[0] = r1 * c2;
+  out[1] = r1 * s2;
+  out[2] = r2 * c4;
 }
 
 /* ------------------------------------------------------------------------ */

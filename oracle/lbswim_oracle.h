@@ -62,6 +62,8 @@ void orc_eigenset(orc_params* p, double tau_s, double tau_b);
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 /* Tumble uniform in (0,1] and three standard normals for (seed, swimmer, step). */
 float orc_rng_uniform(uint64_t seed, uint32_t swimmer, uint64_t step);
+double orc_det_log(double x);
+void orc_det_sincos2pi(double u, double* s, double* c);
 void orc_rng_normal3(uint64_t seed, uint32_t swimmer, uint64_t step, double out[3]);
 
 double orc_peskin_delta(double x);

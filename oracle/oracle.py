@@ -75,6 +75,10 @@ def lib():
         L.orc_rng_uniform.restype = C.c_float
         L.orc_rng_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64]
         L.orc_rng_normal3.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, _D]
+        L.orc_det_log.restype = C.c_double
+        L.orc_det_log.argtypes = [C.c_double]
+        L.orc_det_sincos2pi.argtypes = [C.c_double, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]
         L.orc_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                      C.POINTER(C.c_uint32)]
         L.orc_eigenset.argtypes = [C.POINTER(OrcParams), C.c_double, C.c_double]
