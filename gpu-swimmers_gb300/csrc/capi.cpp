@@ -497,6 +497,67 @@ int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host) {
 }
 
 // ---- System.Step -----------------------------------------------------------------
+// ---- batched ensembles -------------------------------------------------------------
+int lbswim_ensemble_create(lbswim_ensemble** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = reinterpret_cast<lbswim_ensemble*>(ensemble_new());
+  API_END
+}
+
+int lbswim_ensemble_destroy(lbswim_ensemble* ens) {
+  API_BEGIN
+  ensemble_delete(reinterpret_cast<Ensemble*>(ens));
+  API_END
+}
+
+int lbswim_ensemble_set_members(lbswim_ensemble* ens, lbswim_lattice* const* lattices,
+                                lbswim_swimmers* const* swimmers, lbswim_tracers* const* tracers,
+                                int n) {
+  API_BEGIN
+  REQUIRE(ens, "ensemble handle is NULL");
+  REQUIRE(n >= 0 && (n == 0 || lattices), "lattice list is NULL");
+  ensemble_set_members(reinterpret_cast<Ensemble*>(ens),
+                       reinterpret_cast<Lattice* const*>(lattices),
+                       reinterpret_cast<Swimmers* const*>(swimmers),
+                       reinterpret_cast<Tracers* const*>(tracers), n);
+  API_END
+}
+
+int lbswim_ensemble_step(lbswim_ensemble* ens, int nsteps) {
+  API_BEGIN
+  REQUIRE(ens, "ensemble handle is NULL");
+  REQUIRE(nsteps >= 0, "nsteps must be non-negative");
+  ensemble_step(reinterpret_cast<Ensemble*>(ens), nsteps);
+  API_END
+}
+
+int lbswim_ensemble_autotune(lbswim_ensemble* ens) {
+  API_BEGIN
+  REQUIRE(ens, "ensemble handle is NULL");
+  ensemble_autotune(reinterpret_cast<Ensemble*>(ens));
+  API_END
+}
+
+int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(tile, "tile is NULL");
+  *tile = CLAT(lat)->fused_tile;
+  API_END
+}
+
+int lbswim_lattice_set_tile(lbswim_lattice* lat, int tile) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(tile == 0 || tile == 1, "tile must be 0 or 1");
+  Lattice* L = LAT(lat);
+  lattice_join(L);
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  L->fused_tile = tile;
+  API_END
+}
+
 int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, int n_swimmers,
                        lbswim_tracers* const* tracers, int n_tracers, int nsteps) {
   API_BEGIN

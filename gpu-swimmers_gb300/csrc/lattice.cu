@@ -340,8 +340,10 @@ constexpr int fused_smem_bytes() {
                 : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
 
+// One slab: tile (tz, ty, tx) of the lattice in units of (TZ, TY, FUSED_LX)
+// sites; `slab` indexes its bucket of pending ends.  Called by one CTA.
 template <class S, int TZ, int TY, bool SPREAD>
-__global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
+__device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
   constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   float* ringC = ringB + NB * 5 * PLANE;           // [NC][5][PLANE]
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * FUSED_LX;
+  const int z0 = tz * TZ, y0 = ty * TY, x0 = tx * FUSED_LX;
   const int ez = min(TZ, nz - z0), ey = min(TY, ny - y0), ex = min(FUSED_LX, nx - x0);
 
   int ly = 0, lz = 0;
@@ -388,7 +390,6 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
   // the ring threads, which write no output plane, take the first pairs
   const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
   if (SPREAD) {
-    const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     sp.bind(smraw, a.spread, slab, nx, ny, nz, x0, y0, z0, ex, ey, ez);
     sp.prologue(tid, blockDim.x);
     sp.scatter(0, rt, blockDim.x);
@@ -475,6 +476,84 @@ __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(
     Fp2 = cur[17];
     k3 = k3 == 2 ? 0 : k3 + 1;
   }
+}
+
+template <class S, int TZ, int TY, bool SPREAD>
+__global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
+  fused_slab<S, TZ, TY, SPREAD>(a, blockIdx.x, blockIdx.y, blockIdx.z,
+                                (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Batched step of an ensemble of FP32 lattices: one persistent launch takes the
+// slabs of every member from a shared counter (both slab shapes are compiled
+// in; a member's shape is its autotuned choice) and runs the step kernel's
+// per-slab code on each, spreading the member's pending ends.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int ens_member_of(const int* __restrict__ prefix, int nmem, int item) {
+  int lo = 0, hi = nmem - 1;  // last member whose first item is <= item
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+constexpr int ENS_STEP_SMEM =
+    fused_smem_bytes<32, 8, true>() > fused_smem_bytes<16, 16, true>()
+        ? fused_smem_bytes<32, 8, true>()
+        : fused_smem_bytes<16, 16, true>();
+static_assert(8 * 32 == 16 * 16, "both slab shapes use the same block");
+
+__global__ void __launch_bounds__(8 * 32 + FUSED_RING_THREADS, 2) k_ens_step(EnsTable t, int parity) {
+  __shared__ int s_tile;
+  const int nmem = *t.nmem;
+  const int total = t.tile_prefix[nmem];
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&t.counters[parity], 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= total) break;
+    const int m = ens_member_of(t.tile_prefix, nmem, tile);
+    const EnsMember& M = t.mem[m];
+    const int lt = tile - t.tile_prefix[m];
+    const int tz = lt % M.nt[2], ty = (lt / M.nt[2]) % M.nt[1], tx = lt / (M.nt[2] * M.nt[1]);
+    FusedArgs a{};
+    a.f_old = M.f[parity];
+    a.f_new = M.f[parity ^ 1];
+    a.force = nullptr;
+    a.hydro = (float4*)M.hyd[parity];
+    a.nx = M.size[0];
+    a.ny = M.size[1];
+    a.nz = M.size[2];
+    a.n = M.n;
+    a.rho0 = M.rho0;
+    a.k = Relax<float>{M.omega_s, M.omega_b, M.force_s, M.force_b};
+    a.spread = SlabEnds{(const EndRecord<float>*)M.ends, M.bucket_count, M.bucket_list,
+                        2 * M.nsw, M.max_abs_f};
+    if (M.tile == 1)
+      fused_slab<float, 16, 16, true>(a, tz, ty, tx, lt);
+    else
+      fused_slab<float, 32, 8, true>(a, tz, ty, tx, lt);
+    __syncthreads();
+  }
+}
+
+int ens_step_ctas_per_sm() { return 2; }
+
+void ens_launch_step(const EnsTable& t, int parity, int grid, cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    LB_CUDA(cudaFuncSetAttribute(k_ens_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 ENS_STEP_SMEM));
+    configured = true;
+  }
+  k_ens_step<<<grid, 8 * 32 + FUSED_RING_THREADS, ENS_STEP_SMEM, s>>>(t, parity);
+  LB_CHECK_LAUNCH(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -682,11 +761,12 @@ static void fused_step_tile(Lattice* L, FusedArgs& a) {
   }
 }
 
-void fused_slab_shape(const Lattice* L, int T[3]) {
+void slab_shape_of(int tile, int T[3]) {
   T[0] = FUSED_LX;
-  T[1] = L->fused_tile == 1 ? 16 : 8;
-  T[2] = L->fused_tile == 1 ? 16 : 32;
+  T[1] = tile == 1 ? 16 : 8;
+  T[2] = tile == 1 ? 16 : 32;
 }
+void fused_slab_shape(const Lattice* L, int T[3]) { slab_shape_of(L->fused_tile, T); }
 
 template <class S>
 static void fused_step_t(Lattice* L) {

@@ -166,6 +166,72 @@ struct Tracers {
   bool side_pending = false;
 };
 
+// ---- batched ensembles ---------------------------------------------------------
+// One member of a batched ensemble as the batched kernels see it: an FP32
+// lattice with its swimmers and tracers, buffers named relative to the start
+// of the current run.
+struct EnsMember {
+  int size[3];
+  long long n;
+  float rho0;
+  float omega_s, omega_b, force_s, force_b;  // Relax<float>
+  int tile;                                  // slab shape: 0 = 8 x 32, 1 = 16 x 16
+  int nt[3];                                 // slabs per axis
+  void* f[2];           // f(t) at the run's start, and the other buffer
+  void* hyd[2];         // float4 {u, rho} written by steps 0, 2, 4, ... / 1, 3, 5, ...
+  void* ends;           // EndRecord<float>[2 nsw]
+  unsigned* bucket_count;
+  int* bucket_list;
+  unsigned* max_abs_f;
+  int nsw;
+  double* sw_r;
+  double* sw_v;
+  double* sw_n;
+  lbswim_common_params common;
+  unsigned long long seed, step0;  // swimmer RNG key and move step at the run's start
+  int ntr;
+  double* tr_r;
+  double* tr_s;
+  double* tr_v;
+};
+
+// Device tables of an ensemble; the batched kernels of a captured step read
+// everything from here, so membership changes need no new graph.
+struct EnsTable {
+  int* nmem;           // [1]
+  EnsMember* mem;      // [capacity]
+  int* tile_prefix;    // [capacity + 1] first slab of each member
+  int* rec_prefix;     // [capacity + 1] first end-record block
+  int* sw_prefix;      // [capacity + 1] first swimmer-move block
+  int* tr_prefix;      // [capacity + 1] first tracer-move block
+  unsigned* counters;  // [2] slab counters of the two relative parities
+  long long* g_step;   // steps of the current run, -1 before its first
+};
+
+// Work items per block of the batched kernels (particles.cu checks them).
+constexpr int ENS_ENDS_PER_BLOCK = 256;
+constexpr int ENS_SWIMMERS_PER_BLOCK = 64;
+constexpr int ENS_TRACERS_PER_BLOCK = 256;
+
+// Launches of the batched step (lattice.cu, particles.cu).
+void ens_launch_reset(const EnsTable& t, int parity, cudaStream_t s);
+void ens_launch_records(const EnsTable& t, int grid, cudaStream_t s);
+void ens_launch_step(const EnsTable& t, int parity, int grid, cudaStream_t s);
+void ens_launch_move(const EnsTable& t, int parity, int grid, cudaStream_t s);
+int ens_step_ctas_per_sm();
+// Slab shape of a tile choice (x planes, rows, columns).
+void slab_shape_of(int tile, int T[3]);
+
+// ensemble.cpp
+struct Ensemble;
+Ensemble* ensemble_new();
+void ensemble_delete(Ensemble* E);
+void ensemble_set_members(Ensemble* E, Lattice* const* lat, Swimmers* const* sw,
+                          Tracers* const* tr, int n);
+void ensemble_step(Ensemble* E, int nsteps);
+void ensemble_autotune(Ensemble* E);
+int ensemble_size(const Ensemble* E);
+
 // lattice.cu
 void lattice_alloc(Lattice* L);
 void lattice_free(Lattice* L);
@@ -196,6 +262,8 @@ SlabSpread spread_prepare_slabs(Lattice* L);
 // Slab shape of the fused step kernel for a lattice: x planes per slab, rows,
 // columns (lattice.cu).
 void fused_slab_shape(const Lattice* L, int T[3]);
+// Pending-end storage and slab buckets for `nends` ends (particles.cu).
+void spread_reserve(Lattice* L, int nends);
 // Dense force (base + spread of the pending ends) of a reduced-precision
 // lattice, bit for bit the force the step kernel spreads (lattice.cu).
 void lattice_force_from_slabs(Lattice* L);

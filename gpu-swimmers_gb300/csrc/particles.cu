@@ -285,6 +285,13 @@ __device__ __forceinline__ void touched_range(int o, int n, int T, int h, int nt
 
 constexpr int REC_THREADS = 256;
 
+// Slab shape of a tile choice, as slab_shape_of (lattice.cu): x planes, rows, columns.
+__device__ __forceinline__ void slab_shape_of_dev(int tile, int T[3]) {
+  T[0] = 32;
+  T[1] = tile == 1 ? 16 : 8;
+  T[2] = tile == 1 ? 16 : 32;
+}
+
 // One record per dipole end: e = 2i is the tail, 2i + 1 the head.  Records are
 // assembled in shared memory and written out as one contiguous block.
 // List end e under every slab of grid G whose extended region its stencil
@@ -315,15 +322,16 @@ __device__ __forceinline__ void bucket_end(int e, const int o[3], const Dims& D,
 // the stencil origin from the bits of the position (stencil_axis) and the
 // weights of dr - i, like the FP32 interpolation.
 template <class T>
-__global__ void __launch_bounds__(REC_THREADS) k_end_records(
-    int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P, double l,
-    Dims D, EndRecord<T>* __restrict__ ends, int e_base, unsigned* __restrict__ max_abs_f,
-    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list) {
+__device__ __forceinline__ void end_records_block(
+    int blk, int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P,
+    double l, Dims D, EndRecord<T>* __restrict__ ends, int e_base,
+    unsigned* __restrict__ max_abs_f, TileGrid G, unsigned* __restrict__ bucket_count,
+    int* __restrict__ bucket_list) {
   __shared__ EndRecord<T> srec[REC_THREADS];
   __shared__ unsigned smax;
   if (threadIdx.x == 0) smax = 0u;
   __syncthreads();
-  const int e0 = blockIdx.x * REC_THREADS;
+  const int e0 = blk * REC_THREADS;
   const int e = e0 + threadIdx.x;
   const int nends = 2 * nsw;
   if (e < nends) {
@@ -366,6 +374,15 @@ __global__ void __launch_bounds__(REC_THREADS) k_end_records(
   const unsigned* src = reinterpret_cast<const unsigned*>(srec);
   unsigned* dst = reinterpret_cast<unsigned*>(ends + e0);
   for (int w = threadIdx.x; w < words; w += REC_THREADS) dst[w] = src[w];
+}
+
+template <class T>
+__global__ void __launch_bounds__(REC_THREADS) k_end_records(
+    int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P, double l,
+    Dims D, EndRecord<T>* __restrict__ ends, int e_base, unsigned* __restrict__ max_abs_f,
+    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list) {
+  end_records_block<T>(blockIdx.x, nsw, r, nv, P, l, D, ends, e_base, max_abs_f, G, bucket_count,
+                       bucket_list);
 }
 
 // Slab buckets of recorded ends (the slab shape changed since they were recorded).
@@ -930,12 +947,13 @@ __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const
 constexpr int TRACER_MOVE_BLOCK = 256;
 constexpr int TRACER_LANES = 4;  // lanes per interpolation point
 
-__global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
-    int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
-    const float4* __restrict__ h) {
+__device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __restrict__ r,
+                                                   double* __restrict__ s,
+                                                   double* __restrict__ v, Dims D,
+                                                   const float4* __restrict__ h) {
   __shared__ StencilSet<TRACER_MOVE_BLOCK> st;
   __shared__ float3 vel[TRACER_MOVE_BLOCK];
-  const int i = blockIdx.x * TRACER_MOVE_BLOCK + threadIdx.x;
+  const int i = blk * TRACER_MOVE_BLOCK + threadIdx.x;
   const bool valid = i < ntr;
   double rr[3] = {0.0, 0.0, 0.0};
   if (valid) {
@@ -958,21 +976,27 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
   }
 }
 
+__global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
+    int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
+    const float4* __restrict__ h) {
+  tracers_move_block(blockIdx.x, ntr, r, s, v, D, h);
+}
+
 // A block takes SWIMMERS_PER_BLOCK swimmers: two stencils (front and rear
 // point) per swimmer, SWIMMER_LANES threads per stencil.
 constexpr int SWIMMERS_PER_BLOCK = 64;
 constexpr int SWIMMER_LANES = 4;  // lanes per interpolation point
 constexpr int SWIMMER_MOVE_BLOCK = SWIMMERS_PER_BLOCK * SWIMMER_LANES;
 
-__global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
-    int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
-    lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
-    const float4* __restrict__ h) {
+__device__ __forceinline__ void swimmers_move_block(
+    int blk, int nsw, double* __restrict__ swr, double* __restrict__ swv,
+    double* __restrict__ swn, lbswim_common_params c, unsigned long long seed,
+    unsigned long long step, Dims D, const float4* __restrict__ h) {
   constexpr int B = SWIMMERS_PER_BLOCK;
   // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
   __shared__ StencilSet<2 * B> st;
   __shared__ float3 vel[2 * B];
-  const int t = threadIdx.x, i = blockIdx.x * B + t;
+  const int t = threadIdx.x, i = blk * B + t;
   const bool mine = t < B, valid = mine && i < nsw;
   double r[3] = {0.0, 0.0, 0.0};
   float n0[3] = {0.f, 0.f, 0.f};
@@ -1021,6 +1045,107 @@ __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
   }
   const float inv = 1.f / sqrtf(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
   for (int d = 0; d < 3; ++d) swn[nsw * d + i] = f2d_exact(nn[d] * inv);
+}
+
+__global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
+    int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
+    lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
+    const float4* __restrict__ h) {
+  swimmers_move_block(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h);
+}
+
+// ---- batched ensembles: per-step reset, end records, moves --------------------
+__device__ __forceinline__ int ens_find(const int* __restrict__ prefix, int nmem, int item) {
+  int lo = 0, hi = nmem - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ Dims ens_dims(const EnsMember& M) {
+  Dims D;
+  for (int a = 0; a < 3; ++a) {
+    D.n[a] = M.size[a];
+    D.nb[a] = (M.size[a] + BIN - 1) / BIN;
+  }
+  D.N = M.n;
+  return D;
+}
+
+// Zero every member's slab counts and largest |F|, the slab counter of this
+// parity, and advance the run's step counter.
+__global__ void k_ens_reset(EnsTable t, int parity) {
+  const int nmem = *t.nmem;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    t.counters[parity] = 0u;
+    *t.g_step += 1;
+  }
+  for (int m = blockIdx.x; m < nmem; m += gridDim.x) {
+    const EnsMember& M = t.mem[m];
+    const int nslabs = M.nt[0] * M.nt[1] * M.nt[2];
+    for (int i = threadIdx.x; i < nslabs; i += blockDim.x) M.bucket_count[i] = 0u;
+    if (threadIdx.x == 0) *M.max_abs_f = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(REC_THREADS) k_ens_records(EnsTable t) {
+  const int nmem = *t.nmem;
+  const int total = t.rec_prefix[nmem];
+  for (int vb = blockIdx.x; vb < total; vb += gridDim.x) {
+    const int m = ens_find(t.rec_prefix, nmem, vb);
+    const EnsMember& M = t.mem[m];
+    TileGrid G;
+    slab_shape_of_dev(M.tile, G.T);
+    G.h = 1;
+    for (int a = 0; a < 3; ++a) G.nt[a] = M.nt[a];
+    end_records_block<float>(vb - t.rec_prefix[m], M.nsw, M.sw_r, M.sw_n, M.common.P,
+                             M.common.l, ens_dims(M), (EndRecord<float>*)M.ends, 0, M.max_abs_f,
+                             G, M.bucket_count, M.bucket_list);
+    __syncthreads();
+  }
+}
+
+static_assert(SWIMMER_MOVE_BLOCK == TRACER_MOVE_BLOCK, "one block size for both moves");
+static_assert(ENS_ENDS_PER_BLOCK == REC_THREADS && ENS_SWIMMERS_PER_BLOCK == SWIMMERS_PER_BLOCK &&
+                  ENS_TRACERS_PER_BLOCK == TRACER_MOVE_BLOCK,
+              "batched work items per block");
+
+__global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_ens_move(EnsTable t, int parity) {
+  const int nmem = *t.nmem;
+  const int nsb = t.sw_prefix[nmem], total = nsb + t.tr_prefix[nmem];
+  const unsigned long long g = (unsigned long long)*t.g_step;
+  for (int vb = blockIdx.x; vb < total; vb += gridDim.x) {
+    if (vb < nsb) {
+      const int m = ens_find(t.sw_prefix, nmem, vb);
+      const EnsMember& M = t.mem[m];
+      swimmers_move_block(vb - t.sw_prefix[m], M.nsw, M.sw_r, M.sw_v, M.sw_n, M.common, M.seed,
+                          M.step0 + g, ens_dims(M), (const float4*)M.hyd[parity]);
+    } else {
+      const int m = ens_find(t.tr_prefix, nmem, vb - nsb);
+      const EnsMember& M = t.mem[m];
+      tracers_move_block(vb - nsb - t.tr_prefix[m], M.ntr, M.tr_r, M.tr_s, M.tr_v, ens_dims(M),
+                         (const float4*)M.hyd[parity]);
+    }
+    __syncthreads();
+  }
+}
+
+void ens_launch_reset(const EnsTable& t, int parity, cudaStream_t s) {
+  k_ens_reset<<<152, 256, 0, s>>>(t, parity);
+  LB_CHECK_LAUNCH(1);
+}
+void ens_launch_records(const EnsTable& t, int grid, cudaStream_t s) {
+  k_ens_records<<<grid, REC_THREADS, 0, s>>>(t);
+  LB_CHECK_LAUNCH(1);
+}
+void ens_launch_move(const EnsTable& t, int parity, int grid, cudaStream_t s) {
+  k_ens_move<<<grid, TRACER_MOVE_BLOCK, 0, s>>>(t, parity);
+  LB_CHECK_LAUNCH(1);
 }
 
 // ---- host side -----------------------------------------------------------------
@@ -1212,6 +1337,13 @@ static bool ensure_buckets(Lattice* L) {
   S.bucket_slabs = nslabs;
   S.bucket_tile = -1;
   return false;
+}
+
+void spread_reserve(Lattice* L, int nends) {
+  ensure_ends(L, nends);
+  SpreadScratch& S = L->spread;
+  if (!S.max_abs_force) LB_CUDA(cudaMalloc(&S.max_abs_force, sizeof(unsigned)));
+  ensure_buckets(L);
 }
 
 SlabSpread spread_prepare_slabs(Lattice* L) {

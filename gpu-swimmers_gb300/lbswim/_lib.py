@@ -75,6 +75,14 @@ _PROTOS = {
     "lbswim_lattice_set_stream": (C.c_int, [_VP, _VP]),
     "lbswim_lattice_synchronize": (C.c_int, [_VP]),
     "lbswim_lattice_join": (C.c_int, [_VP]),
+    "lbswim_lattice_get_tile": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "lbswim_lattice_set_tile": (C.c_int, [_VP, C.c_int]),
+    "lbswim_ensemble_create": (C.c_int, [C.POINTER(_VP)]),
+    "lbswim_ensemble_destroy": (C.c_int, [_VP]),
+    "lbswim_ensemble_set_members": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP),
+                                              C.POINTER(_VP), C.c_int]),
+    "lbswim_ensemble_step": (C.c_int, [_VP, C.c_int]),
+    "lbswim_ensemble_autotune": (C.c_int, [_VP]),
     "lbswim_lattice_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP), C.POINTER(C.c_int)]),
     "lbswim_lattice_set_timing": (C.c_int, [_VP, C.c_int]),
     "lbswim_lattice_get_timing": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),

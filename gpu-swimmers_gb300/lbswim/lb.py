@@ -200,6 +200,17 @@ class Lattice:
     def synchronize(self):
         _lib.check(_lib.lib.lbswim_lattice_synchronize(self._h))
 
+    @property
+    def tile(self):
+        """Slab shape of the step kernel: 0 = 8 x 32 cross-section, 1 = 16 x 16."""
+        t = C.c_int()
+        _lib.check(_lib.lib.lbswim_lattice_get_tile(self._h, C.byref(t)))
+        return t.value
+
+    @tile.setter
+    def tile(self, value):
+        _lib.check(_lib.lib.lbswim_lattice_set_tile(self._h, int(value)))
+
     def join(self):
         """Order this lattice's stream after the tracer moves that System.Step
         leaves running on the tracers' own streams (no host wait)."""

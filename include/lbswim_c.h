@@ -242,6 +242,29 @@ int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat);
 int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host);
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
 
+/* ---- batched ensembles ------------------------------------------------------
+ * No reference counterpart (the reference steps one lattice at a time).  An
+ * ensemble advances many independent FP32 solves -- each an FP32 lattice with
+ * an optional swimmer array and an optional tracer array, all created and
+ * initialised with the calls above -- by the same coupled step as
+ * lbswim_system_step, in four batched launches per step replayed from a CUDA
+ * graph.  Each member ends exactly where lbswim_system_step would have taken
+ * it (bit for bit, with the same slab shape).  Membership can change between
+ * calls to lbswim_ensemble_step; members stay owned by the caller and must
+ * outlive their membership.  autotune picks, per lattice shape, the slab shape
+ * that runs fastest (timed on scratch copies; results cached per shape). */
+typedef struct lbswim_ensemble lbswim_ensemble;
+int lbswim_ensemble_create(lbswim_ensemble** out);
+int lbswim_ensemble_destroy(lbswim_ensemble* ens);
+int lbswim_ensemble_set_members(lbswim_ensemble* ens, lbswim_lattice* const* lattices,
+                                lbswim_swimmers* const* swimmers, lbswim_tracers* const* tracers,
+                                int n);
+int lbswim_ensemble_step(lbswim_ensemble* ens, int nsteps);
+int lbswim_ensemble_autotune(lbswim_ensemble* ens);
+/* Slab shape of a lattice's step kernel: 0 = 8 x 32 cross-section, 1 = 16 x 16. */
+int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile);
+int lbswim_lattice_set_tile(lbswim_lattice* lat, int tile);
+
 /* ---- coupled step (System.Step, System.py:9-16) ---------------------------- */
 /* nsteps repetitions of: ZeroForce; AddForces for every swimmer array; Step;
  * CalcHydro; Move for every swimmer array, then every tracer array.  Results
