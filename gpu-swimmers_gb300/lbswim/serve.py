@@ -1,0 +1,235 @@
+"""Serving many independent solves on one GPU (no reference counterpart).
+
+A solve is a lattice with its swimmers and tracers advanced a requested
+number of coupled steps.  `Server` keeps a batched Ensemble of the solves in
+flight: arrivals are admitted while their device memory fits an HBM budget,
+every solve in flight advances in the same batched launches, and a solve
+leaves the batch (its slot and memory freed) as soon as it has done its
+steps; solves that arrive while others run join at the next chunk of steps.
+`serve_one_at_a_time` is the plain counterpart: one solve at a time, in
+arrival order, through System.Step.
+
+Solves are drawn from the batched-ensemble distribution: lattice shapes from
+16^3 to 48x48x96 (96^3 and 128^3 added for serving), tau uniform in
+[0.6, 1.5], a swimmer count log-uniform in [1, 512] with P in [1e-4, 1e-3]
+and alpha in [0, 0.05], orientations uniform on the sphere, and a tracer
+count uniform in [0, 4096].  Initial density 1 + 1e-3 U[0, 1), velocity 0.
+"""
+import collections
+import math
+import time
+
+import numpy as np
+
+from . import lb, swimmers, tracers
+from .ensemble import Ensemble
+from .System import System
+
+ENSEMBLE_SHAPES = [(16, 16, 16), (24, 24, 24), (32, 32, 32), (48, 48, 48), (64, 64, 64),
+                   (32, 32, 64), (48, 48, 96)]
+SERVING_SHAPES = ENSEMBLE_SHAPES + [(96, 96, 96), (128, 128, 128)]
+
+
+class Spec:
+    """One solve: lattice shape, relaxation time, particles and seeds."""
+
+    def __init__(self, shape, tau, nsw, P, alpha, ntr, seed, steps=0, l=0.5):
+        self.shape, self.tau, self.nsw, self.P, self.alpha = tuple(shape), tau, nsw, P, alpha
+        self.ntr, self.seed, self.steps, self.l = ntr, seed, steps, l
+
+    @property
+    def sites(self):
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+    def device_bytes(self, precision="f32"):
+        """Device memory of the solve: two f buffers, velocity buffers, force,
+        slab buckets, dipole-end records and particles."""
+        n = self.sites
+        fb = {"f64": 8, "f32": 4}.get(precision, 2)
+        per_site = 2 * 15 * fb + (56 if precision == "f64" else 2 * 16 + 12)
+        slabs = math.ceil(self.shape[0] / 32) * math.ceil(self.shape[1] / 8) * \
+            math.ceil(self.shape[2] / 32) + 64
+        return n * per_site + slabs * 4096 + self.nsw * 300 + self.ntr * 200 + (1 << 16)
+
+
+def draw_spec(rng, shapes=ENSEMBLE_SHAPES, steps_range=None):
+    shape = shapes[rng.integers(len(shapes))]
+    nsw = int(math.floor(math.exp(rng.uniform(0.0, math.log(512.0)))))
+    steps = 0
+    if steps_range:
+        lo, hi = steps_range
+        steps = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    return Spec(shape, float(rng.uniform(0.6, 1.5)), max(1, min(512, nsw)),
+                float(rng.uniform(1e-4, 1e-3)), float(rng.uniform(0.0, 0.05)),
+                int(rng.integers(0, 4097)), int(rng.integers(1, 2**31)), steps)
+
+
+def build_solve(spec, precision="f32"):
+    """Device objects of a solve, initialised from its seed."""
+    rng = np.random.default_rng(spec.seed)
+    nx, ny, nz = spec.shape
+    N = spec.sites
+    lat = lb.Lattice(nx, ny, nz, spec.tau, spec.tau, precision=precision)
+    lat.rho[:] = (1.0 + 1e-3 * rng.random(N)).reshape(1, nx, ny, nz)
+    lat.rho.H2D()
+    lat.u[:] = 0.0
+    lat.u.H2D()
+    lat.InitFromHydro()
+    box = np.array(spec.shape, dtype=np.float64).reshape(3, 1)
+    cp = swimmers.CommonParams()
+    cp.P = spec.P
+    cp.l = spec.l
+    cp.alpha = spec.alpha
+    cp.mobility = (1.0 / 0.1 - 1.0 / 1.5) / (6.0 * np.pi * spec.tau / 3.0)
+    cp.seed = spec.seed
+    sw = swimmers.Array(spec.nsw, cp)
+    sw.r[:] = rng.random((3, spec.nsw)) * box
+    nv = rng.standard_normal((3, spec.nsw))
+    sw.n[:] = nv / np.linalg.norm(nv, axis=0, keepdims=True)
+    sw.v[:] = 0.0
+    sw.H2D()
+    tr = None
+    if spec.ntr > 0:
+        tr = tracers.Array(spec.ntr)
+        tr.r[:] = rng.random((3, spec.ntr)) * box
+        tr.s[:] = 0.0
+        tr.v[:] = 0.0
+        tr.H2D()
+    return lat, sw, tr
+
+
+def poisson_trace(rng, rate, duration, shapes=SERVING_SHAPES, steps_range=(100, 5000)):
+    """Arrival times of a Poisson stream and the solve of each arrival."""
+    t, out = 0.0, []
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            return out
+        out.append((t, draw_spec(rng, shapes, steps_range)))
+
+
+class _Job:
+    def __init__(self, arrival, spec, objs, nbytes):
+        self.arrival, self.spec, self.objs, self.bytes = arrival, spec, objs, nbytes
+        self.remaining = spec.steps
+        self.admitted = None
+
+
+class Server:
+    """Continuous batching of solves under an HBM budget."""
+
+    def __init__(self, budget_bytes, chunk=64, precision="f32", autotune=True):
+        self.budget, self.chunk, self.precision = budget_bytes, chunk, precision
+        self.autotune = autotune
+        self.ens = Ensemble()
+
+    def run(self, trace, duration, drain=False, keep=None):
+        """Serve `trace` (list of (arrival seconds, Spec)) for `duration`
+        seconds of wall time (or until done with drain).  Returns the latency
+        of every finished solve, the site updates done and the wall time;
+        `keep` (a set of trace indices) keeps those solves' objects."""
+        t0 = time.perf_counter()
+        pending = collections.deque((i, a, s) for i, (a, s) in enumerate(trace))
+        waiting, active, done = collections.deque(), [], []
+        used = 0
+        updates = 0
+        kept = {}
+        members_changed = False
+        while True:
+            now = time.perf_counter() - t0
+            if now >= duration and not (drain and (pending or waiting or active)):
+                break
+            while pending and pending[0][1] <= now:
+                waiting.append(pending.popleft())
+            # admission: in arrival order while the next solve fits the budget
+            while waiting and used + waiting[0][2].device_bytes(self.precision) <= self.budget:
+                i, arrival, spec = waiting.popleft()
+                nb = spec.device_bytes(self.precision)
+                job = _Job(arrival, spec, build_solve(spec, self.precision), nb)
+                job.index = i
+                job.admitted = time.perf_counter() - t0
+                used += nb
+                active.append(job)
+                members_changed = True
+            if not active:
+                if waiting and used == 0:
+                    raise RuntimeError("a solve does not fit the HBM budget")
+                nxt = pending[0][1] if pending else None
+                if nxt is None and not waiting:
+                    if drain:
+                        break
+                    time.sleep(max(0.0, min(duration - now, 0.01)))
+                    continue
+                if nxt is not None:
+                    time.sleep(max(0.0, min(nxt - now, duration - now, 0.01)))
+                continue
+            if members_changed:
+                self.ens.set_members([j.objs for j in active])
+                if self.autotune:
+                    self.ens.autotune()
+                members_changed = False
+            k = min(self.chunk, min(j.remaining for j in active))
+            self.ens.Step(k)
+            for j in active:
+                j.remaining -= k
+                updates += j.spec.sites * k
+            finished = [j for j in active if j.remaining <= 0]
+            if finished:
+                t_fin = time.perf_counter() - t0
+                active = [j for j in active if j.remaining > 0]
+                for j in finished:
+                    done.append({"index": j.index, "latency": t_fin - j.arrival,
+                                 "queue": j.admitted - j.arrival, "sites": j.spec.sites,
+                                 "steps": j.spec.steps})
+                    used -= j.bytes
+                    if keep is not None and j.index in keep:
+                        kept[j.index] = j.objs
+                self.ens.set_members([j.objs for j in active])
+        wall = time.perf_counter() - t0
+        return {"done": done, "updates": updates, "wall": wall,
+                "unfinished": len(active) + len(waiting) + len(pending), "kept": kept}
+
+
+def serve_one_at_a_time(trace, duration, precision="f64"):
+    """The plain counterpart: each solve in arrival order through System.Step."""
+    t0 = time.perf_counter()
+    done, updates = [], 0
+    unfinished = 0
+    for i, (arrival, spec) in enumerate(trace):
+        now = time.perf_counter() - t0
+        if now >= duration:
+            unfinished = len(trace) - i
+            break
+        if arrival > now:
+            time.sleep(arrival - now)
+        lat, sw, tr = build_solve(spec, precision)
+        system = System(lat)
+        system.AddThing(sw)
+        if tr is not None:
+            system.AddThing(tr)
+        left = spec.steps
+        while left > 0 and time.perf_counter() - t0 < duration:
+            k = min(left, 64)
+            system.Step(k)
+            lat.synchronize()
+            left -= k
+            updates += spec.sites * k
+        if left > 0:
+            unfinished = len(trace) - i
+            break
+        done.append({"index": i, "latency": time.perf_counter() - t0 - arrival,
+                     "sites": spec.sites, "steps": spec.steps})
+    return {"done": done, "updates": updates, "wall": time.perf_counter() - t0,
+            "unfinished": unfinished}
+
+
+def summary(result):
+    lat = sorted(d["latency"] for d in result["done"])
+
+    def pct(p):
+        if not lat:
+            return None
+        return lat[min(len(lat) - 1, int(math.ceil(p / 100.0 * len(lat))) - 1)]
+    return {"completed": len(lat), "unfinished": result["unfinished"],
+            "p50_s": pct(50), "p99_s": pct(99),
+            "glups": result["updates"] / result["wall"] / 1e9, "wall_s": result["wall"]}
