@@ -365,10 +365,100 @@ def our_arm(args, world, rank, local):
                               "frac": step_ach / peak, "bytes_per_step": step_bytes}}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_port(min(96, side), 12.0)
+    # the batched ensemble and the served stream, each against plain FP64
+    # one solve at a time (every rank runs its own replica)
+    if args.ens_members > 0:
+        line["ensemble"] = ensemble_arm(args)
+    if args.serve_seconds > 0:
+        line["serving"] = serving_arm(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def ensemble_arm(args):
+    """Batched ensemble of independent FP32 solves (shapes 16^3 .. 48x48x96,
+    tau, swimmers and tracers drawn per solve) advanced together, against the
+    same solves stepped one at a time in plain FP64 (stepping timed only)."""
+    import torch
+    from lbswim import serve
+    from lbswim.ensemble import Ensemble
+    from lbswim.System import System
+    rng = np.random.default_rng(7)
+    specs = [serve.draw_spec(rng) for _ in range(args.ens_members)]
+    sites = sum(s.sites for s in specs)
+    objs = [serve.build_solve(s, "f32") for s in specs]
+    ens = Ensemble(objs)
+    ens.autotune()
+    tiles = [o[0].tile for o in objs]
+    ens.Step(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.Step(args.ens_steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    batched = sites * args.ens_steps / dt / 1e9
+    del ens, objs
+    # plain FP64, one solve at a time, the same solves
+    f64_steps, f64_time = args.ens_f64_steps, 0.0
+    for sp in specs:
+        lat, sw, tr = serve.build_solve(sp, "f64")
+        system = System(lat)
+        system.AddThing(sw)
+        if tr is not None:
+            system.AddThing(tr)
+        lat.synchronize()
+        t0 = time.perf_counter()
+        system.Step(f64_steps)
+        lat.synchronize()
+        f64_time += time.perf_counter() - t0
+    plain = sites * f64_steps / f64_time / 1e9
+    # FP32 (batched) against FP64 velocity fields after the full run
+    chk = specs[:4]
+    cobjs = [serve.build_solve(sp, "f32") for sp in chk]
+    cens = Ensemble(cobjs)
+    cens.Step(args.ens_steps)
+    err = 0.0
+    for sp, (lat32, _, _) in zip(chk, cobjs):
+        lat, sw, tr = serve.build_solve(sp, "f64")
+        system = System(lat)
+        system.AddThing(sw)
+        if tr is not None:
+            system.AddThing(tr)
+        system.Step(args.ens_steps)
+        lat.u.D2H()
+        lat32.u.D2H()
+        a, b = lat32.u.data.reshape(3, -1), lat.u.data.reshape(3, -1)
+        err = max(err, float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+    return {"members": len(specs), "sites": sites, "steps": args.ens_steps, "precision": "f32",
+            "batched_glups": batched, "batched_s": dt,
+            "plain_f64_glups": plain, "plain_f64_steps_timed": f64_steps,
+            "speedup_vs_plain_f64": batched / plain,
+            "u_rel_l2_vs_f64": err, "u_check_members": len(chk),
+            "tiles": {"8x32": tiles.count(0), "16x16": tiles.count(1)},
+            "launches_per_step": 4, "graph": "two steps captured, replayed"}
+
+
+def serving_arm(args):
+    """Poisson arrivals of solves (the ensemble distribution plus 96^3 and
+    128^3, steps log-uniform in [100, 5000]) served by continuous batching
+    under an HBM budget, and the same trace served one solve at a time in
+    plain FP64, each for the same wall time."""
+    import torch
+    from lbswim import serve
+    rng = np.random.default_rng(11)
+    trace = serve.poisson_trace(rng, args.serve_rate, args.serve_seconds)
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(0.6 * free)
+    srv = serve.Server(budget, chunk=64)
+    batched = serve.summary(srv.run(trace, args.serve_seconds))
+    del srv
+    plain = serve.summary(serve.serve_one_at_a_time(trace, args.serve_seconds, "f64"))
+    return {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
+            "arrivals": len(trace), "hbm_budget_gb": budget / 1e9, "batched_f32": batched,
+            "plain_f64": plain,
+            "glups_ratio": (batched["glups"] / plain["glups"]) if plain["glups"] else None}
 
 
 def main():
@@ -380,6 +470,14 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f64", "f32", "bf16", "f16"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ens-members", type=int, default=512,
+                    help="batched-ensemble members (0: skip the ensemble figures)")
+    ap.add_argument("--ens-steps", type=int, default=1000)
+    ap.add_argument("--ens-f64-steps", type=int, default=20,
+                    help="steps per solve timed for the plain FP64 rate")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="wall time of each served stream (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()

@@ -539,6 +539,16 @@ int lbswim_ensemble_autotune(lbswim_ensemble* ens) {
   API_END
 }
 
+int lbswim_lattice_conservation(lbswim_lattice* lat, double out[4]) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  Lattice* L = LAT(lat);
+  lattice_join(L);
+  lattice_conservation(L, out);
+  API_END
+}
+
 int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile) {
   API_BEGIN
   check_lattice(lat);

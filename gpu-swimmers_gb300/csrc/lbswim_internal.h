@@ -245,6 +245,8 @@ void lattice_d2h(Lattice* L, int field, double* host);
 void fill_params(lbswim_lbparams* p, double tau_s, double tau_b);
 void lattice_read_timing(Lattice* L, double* total_ms, int* launches);
 void lattice_zero_force(Lattice* L);
+// FP64 totals of mass and momentum (sum of f, sum of c f), deterministic.
+void lattice_conservation(Lattice* L, double out[4]);
 // Make the lattice stream wait for the other-stream readers of `buf` (all
 // readers when buf is null).
 void lattice_wait_readers(Lattice* L, const void* buf);

@@ -200,6 +200,13 @@ class Lattice:
     def synchronize(self):
         _lib.check(_lib.lib.lbswim_lattice_synchronize(self._h))
 
+    def conservation(self):
+        """(mass, momentum x, y, z): sums of f and c f over the lattice in FP64,
+        in a fixed order."""
+        out = (C.c_double * 4)()
+        _lib.check(_lib.lib.lbswim_lattice_conservation(self._h, out))
+        return tuple(out)
+
     @property
     def tile(self):
         """Slab shape of the step kernel: 0 = 8 x 32 cross-section, 1 = 16 x 16."""

@@ -147,6 +147,10 @@ int lbswim_lattice_get_addressing(const lbswim_lattice* lat, lbswim_addressing* 
 int lbswim_lattice_get_time_step(const lbswim_lattice* lat, int* out);
 int lbswim_lattice_set_time_step(lbswim_lattice* lat, int time_step); /* lb.pyx:237-244 */
 int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out);
+/* No reference counterpart: total mass and momentum, sum over sites of
+ * sum_p f_p and sum_p c_p f_p, accumulated in FP64 in a fixed order (the same
+ * bits every call), for conservation checks. */
+int lbswim_lattice_conservation(lbswim_lattice* lat, double out[4]);
 /* No reference counterpart: behaviour switches and stream binding. */
 int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags);
 int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);

@@ -170,3 +170,28 @@ def test_f32_particles_track_oracle(rot_off):
     assert np.abs(gs["sw_v"] - os_["sw_v"]).max() < 1e-6
     assert np.abs(gs["sw_n"] - os_["sw_n"]).max() < 1e-4
     assert np.allclose((gs["sw_n"] ** 2).sum(axis=0), 1.0, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "bf16"])
+def test_fp64_conservation_sums(precision):
+    """Mass and momentum totals in FP64: equal to the sums of the read-back f,
+    the same bits on every call, and conserved by the step (no force)."""
+    case = O.random_case((24, 16, 20), 0, 0, seed=12, u_amp=0.01)
+    lat, sw, tr, system = build_gpu(case, precision)
+    c0 = lat.conservation()
+    assert c0 == lat.conservation()
+    lat.fOld.D2H()
+    f = lat.fOld.data.reshape(15, -1)
+    ci = np.array(lat.params.ci)
+    assert abs(c0[0] - f.sum()) <= 1e-10 * abs(c0[0])
+    for a in range(3):
+        assert abs(c0[1 + a] - (ci[:, a:a + 1] * f).sum()) <= 1e-10 * abs(c0[0])
+    for _ in range(10):
+        lat.ZeroForce()
+        lat.Step()
+        lat.CalcHydro()
+    c1 = lat.conservation()
+    tol = {"f64": 1e-13, "f32": 1e-7, "bf16": 1e-3}[precision]
+    assert abs(c1[0] - c0[0]) <= tol * abs(c0[0])
+    for a in range(3):
+        assert abs(c1[1 + a] - c0[1 + a]) <= tol * abs(c0[0])
