@@ -133,6 +133,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x, world):
+    """The largest x over the ranks of the job (a timing is the slowest rank's)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def emit(line, rank):
+    """Rank 0 prints the job's one JSON line."""
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def build_objects(case, precision):
     from lbswim import lb, swimmers, tracers
     from lbswim.System import System
@@ -311,10 +329,7 @@ def our_arm(args, world, rank, local):
     ms = ev0.elapsed_time(ev1)
     lb_ms, lb_n = lat.read_timing()
     lat.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     ms_step = ms / args.steps
     value = N * args.steps * world / (ms / 1e3) / 1e9
 
@@ -333,10 +348,7 @@ def our_arm(args, world, rank, local):
     d2h += 8 * 4 * N
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world)
     e2e = {"value": N * args.steps * world / e2e_s / 1e9, "unit": "GLUPS",
            "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
            "api": "lbswim.System.Step() + swimmers.Array.D2H() per step (Python -> C ABI)"}
@@ -371,8 +383,7 @@ def our_arm(args, world, rank, local):
         line["ensemble"] = ensemble_arm(args)
     if args.serve_seconds > 0:
         line["serving"] = serving_arm(args)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    emit(line, rank)
     if world > 1:
         torch.distributed.destroy_process_group()
 
