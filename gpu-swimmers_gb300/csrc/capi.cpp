@@ -539,6 +539,14 @@ int lbswim_ensemble_autotune(lbswim_ensemble* ens) {
   API_END
 }
 
+int lbswim_lattice_get_rho0(const lbswim_lattice* lat, double* rho0) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(rho0, "rho0 is NULL");
+  *rho0 = CLAT(lat)->rho0;
+  API_END
+}
+
 int lbswim_lattice_conservation(lbswim_lattice* lat, double out[4]) {
   API_BEGIN
   check_lattice(lat);

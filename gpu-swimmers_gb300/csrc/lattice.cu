@@ -181,17 +181,19 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
 }
 
 // Equilibrium from rho, u, lb.cu:314-371 (compat_sxz reproduces lb.cu:356).
-// rho, u come from the FP64 SoA fields or, when packed is set, the float4 ones.
+// rho, u come from the FP64 SoA fields or, when packed is set, the float4 ones,
+// whose w holds rho - rho_w; it is rewritten as rho - rho0 for the new rho0.
 template <class S>
 __global__ void k_init_from_hydro(const double* __restrict__ rho, const double* __restrict__ u,
-                                  const float4* __restrict__ packed, S* __restrict__ f,
-                                  long long N, double rho0, int compat_sxz) {
+                                  float4* __restrict__ packed, S* __restrict__ f, long long N,
+                                  double rho_w, double rho0, int compat_sxz) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
     double r, ux, uy, uz;
     if (packed) {
       const float4 h = packed[s];
-      r = h.w;
+      r = (double)h.w + rho_w;
+      packed[s].w = (float)(r - rho0);
       ux = h.x;
       uy = h.y;
       uz = h.z;
@@ -223,29 +225,32 @@ __global__ void k_calc_hydro_packed(const S* __restrict__ f, const float* __rest
     hydro_moments(d, R, jx, jy, jz);
     float fx, fy, fz;
     load_force(F, N, s, fx, fy, fz);
-    const float r = rho0 + R;
-    const float inv = 1.0f / r;
-    hydro[s] = make_float4((jx + 0.5f * fx) * inv, (jy + 0.5f * fy) * inv, (jz + 0.5f * fz) * inv, r);
+    const float inv = 1.0f / (rho0 + R);
+    hydro[s] = make_float4((jx + 0.5f * fx) * inv, (jy + 0.5f * fy) * inv, (jz + 0.5f * fz) * inv, R);
   }
 }
 
-// Host FP64 [components][N] <-> packed float4 component c (0-2: u, 3: rho).
+// Host FP64 [components][N] <-> packed float4 component c (0-2: u, 3: rho,
+// held as rho - rho0 so that its float keeps the density's fluctuation).
 __global__ void k_packed_from_f64(const double* __restrict__ src, float* __restrict__ packed,
-                                  long long off, long long cnt, long long N, int rho_field) {
+                                  long long off, long long cnt, long long N, int rho_field,
+                                  double rho0) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
        i += (long long)gridDim.x * blockDim.x) {
     const long long e = off + i;
     const int c = rho_field ? 3 : (int)(e / N);
-    packed[4 * (e % N) + c] = (float)src[i];
+    packed[4 * (e % N) + c] = (float)(rho_field ? src[i] - rho0 : src[i]);
   }
 }
 __global__ void k_packed_to_f64(const float* __restrict__ packed, double* __restrict__ dst,
-                                long long off, long long cnt, long long N, int rho_field) {
+                                long long off, long long cnt, long long N, int rho_field,
+                                double rho0) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt;
        i += (long long)gridDim.x * blockDim.x) {
     const long long e = off + i;
     const int c = rho_field ? 3 : (int)(e / N);
-    dst[i] = (double)packed[4 * (e % N) + c];
+    const double v = (double)packed[4 * (e % N) + c];
+    dst[i] = rho_field ? v + rho0 : v;
   }
 }
 
@@ -463,10 +468,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       S* __restrict__ fn = (S*)a.f_new;
 #pragma unroll
       for (int p = 0; p < 15; ++p) Store<S>::st(fn + p * N + s, stored_from_dev<S>(g[p], p));
-      const float rho = a.rho0 + R;
-      const float inv = 1.0f / rho;
+      const float inv = 1.0f / (a.rho0 + R);
       a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
-                               (jz + 0.5f * Fp2) * inv, rho);
+                               (jz + 0.5f * Fp2) * inv, R);
     }
     // the next plane's collision overwrites the slots just read, and the
     // scatter must be complete before the owners read it
@@ -704,15 +708,16 @@ void lattice_zero_force(Lattice* L) {
 }
 
 template <class S>
-static void init_from_hydro_t(Lattice* L) {
+static void init_from_hydro_t(Lattice* L, double rho_w) {
   const long long N = L->n;
   const int compat = (L->compat & LBSWIM_COMPAT_INIT_SXZ) ? 1 : 0;
   if (L->precision == LBSWIM_F64)
     k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        (const double*)L->rho, (const double*)L->u, nullptr, (S*)L->f[L->cur], N, 0.0, compat);
+        (const double*)L->rho, (const double*)L->u, nullptr, (S*)L->f[L->cur], N, 0.0, 0.0,
+        compat);
   else
     k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        nullptr, nullptr, L->hydro, (S*)L->f[L->cur], N, L->rho0, compat);
+        nullptr, nullptr, L->hydro, (S*)L->f[L->cur], N, rho_w, L->rho0, compat);
   LB_CHECK_LAUNCH(1);
 }
 
@@ -765,7 +770,7 @@ __global__ void k_sums_final(const double* __restrict__ part, double* __restrict
   for (int q = 0; q < 4; ++q) out[q] = t[q];
 }
 
-// out = {sum rho, 0, 0, 0} from the packed velocity buffer (mean_density), or
+// out = {sum (rho - rho0), 0, 0, 0} from the packed velocity buffer, or
 // {mass, momentum} from f.
 template <class S>
 static void sums_t(Lattice* L, bool from_hydro, double out[4]) {
@@ -789,24 +794,26 @@ void lattice_conservation(Lattice* L, double out[4]) {
 }
 
 void lattice_init_from_hydro(Lattice* L) {
+  double rho_w = 0.0;
   if (L->precision != LBSWIM_F64) {
     // store the distributions as deviations from w_p rho0 with rho0 the mean
     // density (as a float): the density part then averages out of them and
     // the stored values carry the flow
     double t[4];
     sums_t<float>(L, true, t);
-    L->rho0 = (double)(float)(t[0] / (double)L->n);
+    rho_w = L->rho0;  // reference of the packed densities just uploaded
+    L->rho0 = (double)(float)(rho_w + t[0] / (double)L->n);
   }
   switch (L->precision) {
     case LBSWIM_F64:
       if (L->compat & LBSWIM_COMPAT_EXACT_F64)
         exact_init_from_hydro_f64(L);
       else
-        init_from_hydro_t<double>(L);
+        init_from_hydro_t<double>(L, 0.0);
       break;
-    case LBSWIM_F32: init_from_hydro_t<float>(L); break;
-    case LBSWIM_BF16: init_from_hydro_t<__nv_bfloat16>(L); break;
-    default: init_from_hydro_t<__half>(L); break;
+    case LBSWIM_F32: init_from_hydro_t<float>(L, rho_w); break;
+    case LBSWIM_BF16: init_from_hydro_t<__nv_bfloat16>(L, rho_w); break;
+    default: init_from_hydro_t<__half>(L, rho_w); break;
   }
   L->f_version++;
 }
@@ -1060,7 +1067,7 @@ void lattice_h2d(Lattice* L, int field, const double* host) {
         k_f64_to_f32<<<grid_for(c, 256), 256, 0, L->stream>>>(st, (float*)dst + off, c);
       else
         k_packed_from_f64<<<grid_for(c, 256), 256, 0, L->stream>>>(
-            st, (float*)L->hydro, off, c, L->n, field == LBSWIM_FIELD_RHO);
+            st, (float*)L->hydro, off, c, L->n, field == LBSWIM_FIELD_RHO, L->rho0);
       LB_CHECK_LAUNCH(1);
     }
   }
@@ -1092,7 +1099,7 @@ void lattice_d2h(Lattice* L, int field, double* host) {
       k_f32_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>((const float*)src + off, st, c);
     else
       k_packed_to_f64<<<grid_for(c, 256), 256, 0, L->stream>>>(
-          (const float*)L->hydro, st, off, c, L->n, field == LBSWIM_FIELD_RHO);
+          (const float*)L->hydro, st, off, c, L->n, field == LBSWIM_FIELD_RHO, L->rho0);
     LB_CHECK_LAUNCH(1);
     LB_CUDA(cudaMemcpyAsync(host + off, st, c * sizeof(double), cudaMemcpyDeviceToHost,
                             L->stream));

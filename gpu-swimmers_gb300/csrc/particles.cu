@@ -839,18 +839,35 @@ __device__ __forceinline__ double advance_position(double r, float v, int n) {
   return wrap_position<float>(r + f2d_exact(v), n);
 }
 
-// Three normal deviates of a tumble in FP32 from the counter blocks of
-// rng_normal3 (Box-Muller on 24-bit uniforms in (0, 1]).
+// The 53-bit uniform of rng_normal3 rounded to FP32 (relative error 2^-24 at
+// every magnitude, so the logarithm of a small draw stays close to FP64's).
+__device__ __forceinline__ float u53f(uint32_t a, uint32_t b) {
+  const unsigned long long m = ((unsigned long long)a << 21) | (unsigned long long)(b >> 11);
+  return __ull2float_rn(m + 1ull) * 0x1.0p-53f;
+}
+
+// -2 log u of that uniform in FP32; for u >= 1/2 through log1p of the exact
+// 1 - u, so that draws near 1 keep their small logarithm.
+__device__ __forceinline__ float neg2log_u53(uint32_t a, uint32_t b) {
+  const unsigned long long m1 =
+      (((unsigned long long)a << 21) | (unsigned long long)(b >> 11)) + 1ull;  // 1 .. 2^53
+  if (m1 >= (1ull << 52))
+    return -2.f * log1pf(-__ull2float_rn((1ull << 53) - m1) * 0x1.0p-53f);
+  return -2.f * logf(__ull2float_rn(m1) * 0x1.0p-53f);
+}
+
+// Three normal deviates of a tumble in FP32 from the counter blocks and the
+// uniforms of rng_normal3 (Box-Muller).
 __device__ __forceinline__ void rng_normal3_f(uint64_t seed, uint32_t swimmer, uint64_t step,
                                               float g[3]) {
   uint32_t a[4], b[4];
   rng_block(seed, swimmer, step, 1u, a);
   rng_block(seed, swimmer, step, 2u, b);
-  const float r1 = sqrtf(-2.f * logf((float)((a[0] >> 8) + 1u) * 0x1.0p-24f));
-  const float r2 = sqrtf(-2.f * logf((float)((b[0] >> 8) + 1u) * 0x1.0p-24f));
+  const float r1 = sqrtf(neg2log_u53(a[0], a[1]));
+  const float r2 = sqrtf(neg2log_u53(b[0], b[1]));
   float s1, c1, s2, c2;
-  sincospif((float)((a[2] >> 8) + 1u) * 0x1.0p-23f, &s1, &c1);
-  sincospif((float)((b[2] >> 8) + 1u) * 0x1.0p-23f, &s2, &c2);
+  sincospif(2.f * u53f(a[2], a[3]), &s1, &c1);
+  sincospif(2.f * u53f(b[2], b[3]), &s2, &c2);
   g[0] = r1 * c1;
   g[1] = r1 * s1;
   g[2] = r2 * c2;
@@ -998,11 +1015,11 @@ __device__ __forceinline__ void swimmers_move_block(
   __shared__ float3 vel[2 * B];
   const int t = threadIdx.x, i = blk * B + t;
   const bool mine = t < B, valid = mine && i < nsw;
-  double r[3] = {0.0, 0.0, 0.0};
+  double r[3] = {0.0, 0.0, 0.0}, nd[3] = {0.0, 0.0, 0.0};
   float n0[3] = {0.f, 0.f, 0.f};
   bool tumble = false, rotate = false;
   if (valid) {
-    double nd[3], rMinus[3];
+    double rMinus[3];
     for (int d = 0; d < 3; ++d) {
       r[d] = swr[nsw * d + i];
       nd[d] = swn[nsw * d + i];
@@ -1034,17 +1051,25 @@ __device__ __forceinline__ void swimmers_move_block(
     swv[nsw * d + i] = f2d_exact(rDot);
     swr[nsw * d + i] = advance_position(r[d], rDot, D.n[d]);
   }
-  float nn[3];
   if (tumble) {
+    float nn[3];
     rng_normal3_f(seed, (uint32_t)i, step, nn);
+    const float inv = 1.f / sqrtf(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+    for (int d = 0; d < 3; ++d) swn[nsw * d + i] = f2d_exact(nn[d] * inv);
   } else if (rotate) {
+    // the small turn (v - v_rear) / l is formed in FP32 and added to the FP64
+    // orientation, which keeps its direction; the FP32 norm only rescales it
     const float inv_l = 1.f / (float)c.l;
-    for (int d = 0; d < 3; ++d) nn[d] = n0[d] + (v[d] - vm[d]) * inv_l;
-  } else {
-    return;
+    double nn[3];
+    float sq = 0.f;
+    for (int d = 0; d < 3; ++d) {
+      nn[d] = __dadd_rn(nd[d], f2d_exact((v[d] - vm[d]) * inv_l));
+      const float q = (float)nn[d];
+      sq += q * q;
+    }
+    const double inv = f2d_exact(1.f / sqrtf(sq));
+    for (int d = 0; d < 3; ++d) swn[nsw * d + i] = __dmul_rn(nn[d], inv);
   }
-  const float inv = 1.f / sqrtf(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
-  for (int d = 0; d < 3; ++d) swn[nsw * d + i] = f2d_exact(nn[d] * inv);
 }
 
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(

@@ -77,6 +77,7 @@ _PROTOS = {
     "lbswim_lattice_join": (C.c_int, [_VP]),
     "lbswim_lattice_get_tile": (C.c_int, [_VP, C.POINTER(C.c_int)]),
     "lbswim_lattice_conservation": (C.c_int, [_VP, _D]),
+    "lbswim_lattice_get_rho0": (C.c_int, [_VP, _D]),
     "lbswim_lattice_set_tile": (C.c_int, [_VP, C.c_int]),
     "lbswim_ensemble_create": (C.c_int, [C.POINTER(_VP)]),
     "lbswim_ensemble_destroy": (C.c_int, [_VP]),

@@ -200,6 +200,13 @@ class Lattice:
     def synchronize(self):
         _lib.check(_lib.lib.lbswim_lattice_synchronize(self._h))
 
+    @property
+    def rho0(self):
+        """Reference density of the reduced-precision storage (0 for FP64)."""
+        v = C.c_double()
+        _lib.check(_lib.lib.lbswim_lattice_get_rho0(self._h, C.byref(v)))
+        return v.value
+
     def conservation(self):
         """(mass, momentum x, y, z): sums of f and c f over the lattice in FP64,
         in a fixed order."""

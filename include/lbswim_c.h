@@ -161,8 +161,12 @@ int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
 int lbswim_lattice_synchronize(lbswim_lattice* lat);
 int lbswim_lattice_join(lbswim_lattice* lat);
 /* Device address and element size of a field's current buffer: 8 (FP64
- * lattices); for FP32/BF16/FP16 lattices fOld/fNew are 4 or 2 bytes, force 4,
- * and rho and u share one buffer of float4 {ux, uy, uz, rho} per site (16). */
+ * lattices); for FP32/BF16/FP16 lattices fOld/fNew are 4 or 2 bytes (f - w_p
+ * rho0, divided by w_p for the 16-bit formats), force 4, and rho and u share
+ * one buffer of float4 {ux, uy, uz, rho - rho0} per site (16).  rho0 (no
+ * reference counterpart) is 1 until InitFromHydro sets it to the mean
+ * density, as a float; FP64 lattices have rho0 = 0. */
+int lbswim_lattice_get_rho0(const lbswim_lattice* lat, double* rho0);
 int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, int* elem_bytes);
 /* When enabled, every LB step kernel of this lattice is bracketed by CUDA
  * events on the lattice's stream.  get_timing synchronises the stream and
