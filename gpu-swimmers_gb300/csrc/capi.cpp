@@ -497,6 +497,49 @@ int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host) {
 }
 
 // ---- System.Step -----------------------------------------------------------------
+// ---- seeded initial states -------------------------------------------------------
+int lbswim_lattice_init_random(lbswim_lattice* lat, unsigned long long seed, double amplitude) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(std::isfinite(amplitude), "amplitude must be finite");
+  Lattice* L = LAT(lat);
+  lattice_join(L);
+  lattice_init_random(L, seed, amplitude);
+  API_END
+}
+
+int lbswim_swimmers_init_random(lbswim_swimmers* sw, const lbswim_lattice* lat,
+                                unsigned long long seed) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  check_lattice(lat);
+  swimmers_init_random(reinterpret_cast<Swimmers*>(sw), CLAT(lat), seed);
+  API_END
+}
+
+int lbswim_tracers_init_random(lbswim_tracers* tr, const lbswim_lattice* lat,
+                               unsigned long long seed) {
+  API_BEGIN
+  REQUIRE(tr, "tracers handle is NULL");
+  check_lattice(lat);
+  tracers_init_random(reinterpret_cast<Tracers*>(tr), CLAT(lat), seed);
+  API_END
+}
+
+int lbswim_lattice_set_tau(lbswim_lattice* lat, double tau_s, double tau_b) {
+  API_BEGIN
+  check_lattice(lat);
+  REQUIRE(std::isfinite(tau_s) && std::isfinite(tau_b) && tau_s > -0.5 && tau_b > -0.5,
+          "relaxation times must be finite and > -1/2");
+  Lattice* L = LAT(lat);
+  lattice_join(L);
+  LB_CUDA(cudaStreamSynchronize(L->stream));
+  L->tau_s = tau_s;
+  L->tau_b = tau_b;
+  fill_params(&L->params, tau_s, tau_b);
+  API_END
+}
+
 // ---- batched ensembles -------------------------------------------------------------
 int lbswim_ensemble_create(lbswim_ensemble** out) {
   API_BEGIN

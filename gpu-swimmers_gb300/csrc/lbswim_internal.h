@@ -283,6 +283,9 @@ void tracers_free(Tracers* T);
 void tracers_h2d(Tracers* T, int field, const double* host);
 void tracers_d2h(Tracers* T, int field, double* host);
 void lattice_interp_velocity(Lattice* L, int npoints, const double* r_host, double* v_host);
+void lattice_init_random(Lattice* L, unsigned long long seed, double amp);
+void swimmers_init_random(Swimmers* W, const Lattice* L, unsigned long long seed);
+void tracers_init_random(Tracers* T, const Lattice* L, unsigned long long seed);
 void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,
                double* g_host);
 void spread_forces_noalloc(const double* r, const double* nv, int nsw, double P, double l,

@@ -741,6 +741,56 @@ __global__ void k_rng_draws(unsigned long long seed, int n, unsigned long long s
   for (int d = 0; d < 3; ++d) g[n * d + i] = nn[d];
 }
 
+// ---- seeded initial states made on the device ------------------------------------
+// Counter streams keyed (seed, index) at steps far above any move step:
+// INIT_STEP_SITE for densities, INIT_STEP_PART for particle positions and
+// orientations (block 0: position uniforms, blocks 1-2: orientation normals).
+constexpr unsigned long long INIT_STEP_SITE = 0xffffffffffff0001ull;
+constexpr unsigned long long INIT_STEP_PART = 0xffffffffffff0002ull;
+
+__global__ void k_init_density(long long N, unsigned long long seed, double amp, double rho0,
+                               double* __restrict__ rho, double* __restrict__ u,
+                               float4* __restrict__ hydro) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
+       s += (long long)gridDim.x * blockDim.x) {
+    uint32_t x[4];
+    rng_block(seed, (uint32_t)s, INIT_STEP_SITE, (uint32_t)(s >> 32), x);
+    const double r = 1.0 + amp * (u53(x[0], x[1]) - 0x1.0p-53);  // 1 + amp U[0, 1)
+    if (hydro) {
+      hydro[s] = make_float4(0.f, 0.f, 0.f, (float)(r - rho0));
+    } else {
+      rho[s] = r;
+      u[s] = u[N + s] = u[2 * N + s] = 0.0;
+    }
+  }
+}
+
+// Positions uniform in the box; orientations (when nv is set) uniform on the sphere.
+__global__ void k_init_particles(int n, unsigned long long seed, Dims D, double* __restrict__ r,
+                                 double* __restrict__ nv, double* __restrict__ zero_a,
+                                 double* __restrict__ zero_b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t x[4];
+  rng_block(seed, (uint32_t)i, INIT_STEP_PART, 0u, x);
+  const double ux = u53(x[0], x[1]) - 0x1.0p-53, uy = u53(x[2], x[3]) - 0x1.0p-53;
+  rng_block(seed, (uint32_t)i, INIT_STEP_PART, 3u, x);
+  const double uz = u53(x[0], x[1]) - 0x1.0p-53;
+  const double uu[3] = {ux, uy, uz};
+  for (int d = 0; d < 3; ++d) {
+    r[(long long)n * d + i] = uu[d] * D.n[d];
+    if (zero_a) zero_a[(long long)n * d + i] = 0.0;
+    if (zero_b) zero_b[(long long)n * d + i] = 0.0;
+  }
+  if (nv) {
+    double g[3];
+    rng_normal3(seed, (uint32_t)i, INIT_STEP_PART, g);
+    const double norm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(g[0], g[0]), __dmul_rn(g[1], g[1])),
+                                             __dmul_rn(g[2], g[2])));
+    for (int d = 0; d < 3; ++d) nv[(long long)n * d + i] = g[d] / norm;
+  }
+}
+
 // ---- FP32-path Move kernels ------------------------------------------------------
 // A block moves NP particles in three phases.  (1) One thread per particle forms
 // its stencil -- wrapped origin node and Peskin weights -- in shared memory.
@@ -1761,6 +1811,42 @@ void spread_forces_noalloc(const double* r, const double* nv, int nsw, double P,
   k_spread_gather<double><<<grid, dim3(32, 8), 0, stream>>>(D, ends, bin_start, order, force,
                                                             accumulate);
   LB_CHECK_LAUNCH(1);
+}
+
+void lattice_init_random(Lattice* L, unsigned long long seed, double amp) {
+  const bool packed = L->precision != LBSWIM_F64;
+  if (packed) L->rho0 = 1.0;  // as a new lattice: the same stored bits whatever came before
+  k_init_density<<<(int)std::min<long long>((L->n + 255) / 256, 152LL * 32), 256, 0, L->stream>>>(
+      L->n, seed, amp, L->rho0, packed ? nullptr : (double*)L->rho,
+      packed ? nullptr : (double*)L->u, packed ? L->hydro : nullptr);
+  LB_CHECK_LAUNCH(1);
+  L->shadow_f_version = 0;
+  lattice_init_from_hydro(L);
+}
+
+void swimmers_init_random(Swimmers* W, const Lattice* L, unsigned long long seed) {
+  LB_CUDA(cudaDeviceSynchronize());
+  if (W->n > 0) {
+    k_init_particles<<<(W->n + 255) / 256, 256>>>(W->n, seed, make_dims(L), W->r, W->nv, W->v,
+                                                   nullptr);
+    LB_CHECK_LAUNCH(1);
+  }
+  LB_CUDA(cudaDeviceSynchronize());
+}
+
+void tracers_init_random(Tracers* T, const Lattice* L, unsigned long long seed) {
+  LB_CUDA(cudaDeviceSynchronize());
+  if (T->n > 0) {
+    // user order = work order until the next re-binning
+    k_iota<<<(T->n + 255) / 256, 256>>>(T->n, T->perm);
+    k_init_particles<<<(T->n + 255) / 256, 256>>>(T->n, seed, make_dims(L), T->r, nullptr, T->s,
+                                                   T->v);
+    LB_CHECK_LAUNCH(2);
+    T->identity = true;
+    T->needs_sort = true;
+    T->moves_since_sort = 0;
+  }
+  LB_CUDA(cudaDeviceSynchronize());
 }
 
 void rng_draws(unsigned long long seed, int n, unsigned long long step, float* u_host,

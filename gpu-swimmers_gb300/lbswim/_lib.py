@@ -78,6 +78,10 @@ _PROTOS = {
     "lbswim_lattice_get_tile": (C.c_int, [_VP, C.POINTER(C.c_int)]),
     "lbswim_lattice_conservation": (C.c_int, [_VP, _D]),
     "lbswim_lattice_get_rho0": (C.c_int, [_VP, _D]),
+    "lbswim_lattice_init_random": (C.c_int, [_VP, C.c_ulonglong, C.c_double]),
+    "lbswim_swimmers_init_random": (C.c_int, [_VP, _VP, C.c_ulonglong]),
+    "lbswim_tracers_init_random": (C.c_int, [_VP, _VP, C.c_ulonglong]),
+    "lbswim_lattice_set_tau": (C.c_int, [_VP, C.c_double, C.c_double]),
     "lbswim_lattice_set_tile": (C.c_int, [_VP, C.c_int]),
     "lbswim_ensemble_create": (C.c_int, [C.POINTER(_VP)]),
     "lbswim_ensemble_destroy": (C.c_int, [_VP]),

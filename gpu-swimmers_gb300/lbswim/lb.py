@@ -207,6 +207,15 @@ class Lattice:
         _lib.check(_lib.lib.lbswim_lattice_get_rho0(self._h, C.byref(v)))
         return v.value
 
+    def init_random(self, seed, amplitude=1e-3):
+        """rho = 1 + amplitude U[0, 1), u = 0 from a counter stream keyed by
+        (seed, site), made on the device, then InitFromHydro."""
+        _lib.check(_lib.lib.lbswim_lattice_init_random(self._h, int(seed), float(amplitude)))
+
+    def set_tau(self, tau_s, tau_b):
+        _lib.check(_lib.lib.lbswim_lattice_set_tau(self._h, float(tau_s), float(tau_b)))
+        self._params = None
+
     def conservation(self):
         """(mass, momentum x, y, z): sums of f and c f over the lattice in FP64,
         in a fixed order."""

@@ -21,7 +21,7 @@ import time
 
 import numpy as np
 
-from . import lb, swimmers, tracers
+from . import _lib, lb, swimmers, tracers
 from .ensemble import Ensemble
 from .System import System
 
@@ -64,18 +64,19 @@ def draw_spec(rng, shapes=ENSEMBLE_SHAPES, steps_range=None):
                 int(rng.integers(0, 4097)), int(rng.integers(1, 2**31)), steps)
 
 
-def build_solve(spec, precision="f32"):
-    """Device objects of a solve, initialised from its seed."""
-    rng = np.random.default_rng(spec.seed)
+def build_solve(spec, precision="f32", lattice=None):
+    """Device objects of a solve, initialised on the device from its seed
+    (rho = 1 + 1e-3 U[0, 1), u = 0, particles uniform in the box, swimmer
+    orientations uniform on the sphere).  `lattice`, of the solve's shape and
+    precision, is reused when given."""
     nx, ny, nz = spec.shape
-    N = spec.sites
-    lat = lb.Lattice(nx, ny, nz, spec.tau, spec.tau, precision=precision)
-    lat.rho[:] = (1.0 + 1e-3 * rng.random(N)).reshape(1, nx, ny, nz)
-    lat.rho.H2D()
-    lat.u[:] = 0.0
-    lat.u.H2D()
-    lat.InitFromHydro()
-    box = np.array(spec.shape, dtype=np.float64).reshape(3, 1)
+    if lattice is None:
+        lat = lb.Lattice(nx, ny, nz, spec.tau, spec.tau, precision=precision)
+    else:
+        lat = lattice
+        lat.set_tau(spec.tau, spec.tau)
+        _lib.check(_lib.lib.lbswim_lattice_set_time_step(lat._h, 0))
+    lat.init_random(spec.seed)
     cp = swimmers.CommonParams()
     cp.P = spec.P
     cp.l = spec.l
@@ -83,18 +84,11 @@ def build_solve(spec, precision="f32"):
     cp.mobility = (1.0 / 0.1 - 1.0 / 1.5) / (6.0 * np.pi * spec.tau / 3.0)
     cp.seed = spec.seed
     sw = swimmers.Array(spec.nsw, cp)
-    sw.r[:] = rng.random((3, spec.nsw)) * box
-    nv = rng.standard_normal((3, spec.nsw))
-    sw.n[:] = nv / np.linalg.norm(nv, axis=0, keepdims=True)
-    sw.v[:] = 0.0
-    sw.H2D()
+    sw.init_random(lat, spec.seed)
     tr = None
     if spec.ntr > 0:
         tr = tracers.Array(spec.ntr)
-        tr.r[:] = rng.random((3, spec.ntr)) * box
-        tr.s[:] = 0.0
-        tr.v[:] = 0.0
-        tr.H2D()
+        tr.init_random(lat, spec.seed + 1)
     return lat, sw, tr
 
 
@@ -116,12 +110,21 @@ class _Job:
 
 
 class Server:
-    """Continuous batching of solves under an HBM budget."""
+    """Continuous batching of solves under an HBM budget.
 
-    def __init__(self, budget_bytes, chunk=64, precision="f32", autotune=True):
+    A solve is admitted (in arrival order) while its device memory fits the
+    budget and the sites in flight stay within `max_sites` (beyond the point
+    where the GPU is full, more solves in the batch only lengthen every
+    solve's time).  Lattices of finished solves are kept, per shape, for the
+    next solve of that shape; kept lattices count against the budget and are
+    released when a solve of another shape needs the memory."""
+
+    def __init__(self, budget_bytes, chunk=64, precision="f32", autotune=True,
+                 max_sites=64 << 20):
         self.budget, self.chunk, self.precision = budget_bytes, chunk, precision
-        self.autotune = autotune
+        self.autotune, self.max_sites = autotune, max_sites
         self.ens = Ensemble()
+        self.pool = collections.defaultdict(list)  # shape -> [(lattice, bytes)]
 
     def run(self, trace, duration, drain=False, keep=None):
         """Serve `trace` (list of (arrival seconds, Spec)) for `duration`
@@ -131,24 +134,47 @@ class Server:
         t0 = time.perf_counter()
         pending = collections.deque((i, a, s) for i, (a, s) in enumerate(trace))
         waiting, active, done = collections.deque(), [], []
-        used = 0
+        used = sum(nb for lst in self.pool.values() for _, nb in lst)  # kept lattices
+        sites_in_flight = 0
         updates = 0
         kept = {}
         members_changed = False
+
+        def fits(spec):
+            nonlocal used
+            nb = spec.device_bytes(self.precision)
+            if active and sites_in_flight + spec.sites > self.max_sites:
+                return False
+            if self.pool.get(spec.shape):
+                return True  # a kept lattice of this shape
+            while used + nb > self.budget:
+                victims = [k for k, v in self.pool.items() if v]
+                if not victims:
+                    return False
+                _, vb = self.pool[victims[0]].pop()
+                used -= vb
+            return True
+
         while True:
             now = time.perf_counter() - t0
             if now >= duration and not (drain and (pending or waiting or active)):
                 break
             while pending and pending[0][1] <= now:
                 waiting.append(pending.popleft())
-            # admission: in arrival order while the next solve fits the budget
-            while waiting and used + waiting[0][2].device_bytes(self.precision) <= self.budget:
+            # admission: in arrival order while the next solve fits
+            while waiting and fits(waiting[0][2]):
                 i, arrival, spec = waiting.popleft()
-                nb = spec.device_bytes(self.precision)
-                job = _Job(arrival, spec, build_solve(spec, self.precision), nb)
+                if self.pool.get(spec.shape):
+                    lat, nb = self.pool[spec.shape].pop()
+                    objs = build_solve(spec, self.precision, lattice=lat)
+                else:
+                    nb = spec.device_bytes(self.precision)
+                    objs = build_solve(spec, self.precision)
+                    used += nb
+                job = _Job(arrival, spec, objs, nb)
                 job.index = i
                 job.admitted = time.perf_counter() - t0
-                used += nb
+                sites_in_flight += spec.sites
                 active.append(job)
                 members_changed = True
             if not active:
@@ -181,9 +207,12 @@ class Server:
                     done.append({"index": j.index, "latency": t_fin - j.arrival,
                                  "queue": j.admitted - j.arrival, "sites": j.spec.sites,
                                  "steps": j.spec.steps})
-                    used -= j.bytes
+                    sites_in_flight -= j.spec.sites
                     if keep is not None and j.index in keep:
                         kept[j.index] = j.objs
+                        used -= j.bytes
+                    else:
+                        self.pool[j.spec.shape].append((j.objs[0], j.bytes))
                 self.ens.set_members([j.objs for j in active])
         wall = time.perf_counter() - t0
         return {"done": done, "updates": updates, "wall": wall,

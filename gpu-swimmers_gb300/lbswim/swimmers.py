@@ -102,6 +102,11 @@ class Array:
             _lib.lib.lbswim_swimmers_destroy(h)
             self._h = None
 
+    def init_random(self, lat, seed):
+        """Positions uniform in lat's box, orientations uniform on the sphere,
+        v = 0, made on the device from (seed, swimmer)."""
+        _lib.check(_lib.lib.lbswim_swimmers_init_random(self._h, lat._h, int(seed)))
+
     def AddForces(self, lat):
         _lib.check(_lib.lib.lbswim_swimmers_add_forces(self._h, lat._h))
 

@@ -40,6 +40,10 @@ class Array:
     def AddForces(self, lat):
         """Tracers exert no force (tracers.pyx:20-21)."""
 
+    def init_random(self, lat, seed):
+        """Positions uniform in lat's box, s = v = 0, made on the device."""
+        _lib.check(_lib.lib.lbswim_tracers_init_random(self._h, lat._h, int(seed)))
+
     def Move(self, lat):
         _lib.check(_lib.lib.lbswim_tracers_move(self._h, lat._h))
 

@@ -250,6 +250,21 @@ int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat);
 int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host);
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
 
+/* ---- seeded initial states made on the device --------------------------------
+ * No reference counterpart: for many short solves (serving), whose inputs need
+ * not come from the host.  init_random sets rho = 1 + amplitude U[0, 1) and
+ * u = 0 from a counter stream keyed by (seed, site), then InitFromHydro;
+ * particles get positions uniform in the lattice's box (swimmers also
+ * orientations uniform on the sphere, v = 0; tracers s = v = 0).  The same
+ * seed gives the same state on any lattice precision. */
+int lbswim_lattice_init_random(lbswim_lattice* lat, unsigned long long seed, double amplitude);
+int lbswim_swimmers_init_random(lbswim_swimmers* sw, const lbswim_lattice* lat,
+                                unsigned long long seed);
+int lbswim_tracers_init_random(lbswim_tracers* tr, const lbswim_lattice* lat,
+                               unsigned long long seed);
+/* Relaxation times of an existing lattice (reuse of a lattice for a new solve). */
+int lbswim_lattice_set_tau(lbswim_lattice* lat, double tau_s, double tau_b);
+
 /* ---- batched ensembles ------------------------------------------------------
  * No reference counterpart (the reference steps one lattice at a time).  An
  * ensemble advances many independent FP32 solves -- each an FP32 lattice with

@@ -49,3 +49,25 @@ def test_summary_reports_latency_percentiles():
     s = serve.summary(res)
     assert s["completed"] == 100 and s["unfinished"] == 3
     assert s["p50_s"] == 50.0 and s["p99_s"] == 99.0 and s["glups"] == 0.5
+
+
+def test_device_initial_state_is_seeded_and_precision_independent():
+    from lbswim import lb, swimmers, tracers
+    states = []
+    for precision in ("f64", "f32"):
+        lat = lb.Lattice(20, 12, 16, 0.9, 0.9, precision=precision)
+        lat.init_random(77)
+        sw = swimmers.Array(50, swimmers.CommonParams())
+        sw.init_random(lat, 77)
+        tr = tracers.Array(80)
+        tr.init_random(lat, 78)
+        lat.rho.D2H()
+        sw.D2H()
+        tr.D2H()
+        states.append((lat.rho.data.copy(), sw.r.data.copy(), sw.n.data.copy(), tr.r.data.copy()))
+    (rho64, r64, n64, t64), (rho32, r32, n32, t32) = states
+    assert np.all((rho64 >= 1.0) & (rho64 < 1.001))
+    assert np.abs(rho32 - rho64).max() < 1e-9
+    assert np.array_equal(r64, r32) and np.array_equal(n64, n32) and np.array_equal(t64, t32)
+    assert np.allclose((n64 ** 2).sum(axis=0), 1.0, atol=1e-14)
+    assert np.all(r64 >= 0) and np.all(r64[0] < 20) and np.all(r64[1] < 12) and np.all(r64[2] < 16)
