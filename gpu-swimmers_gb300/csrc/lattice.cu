@@ -347,7 +347,9 @@ constexpr int fused_smem_bytes() {
 
 // One slab: tile (tz, ty, tx) of the lattice in units of (TZ, TY, FUSED_LX)
 // sites; `slab` indexes its bucket of pending ends.  Called by one CTA.
-template <class S, int TZ, int TY, bool SPREAD>
+// I is the site-index type: int when 15 N fits it (one multiply-add per
+// address), long long otherwise.
+template <class S, int TZ, int TY, bool SPREAD, class I = long long>
 __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
@@ -384,8 +386,8 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
     }
   }
   const int gy = wrap_once(y0 + ly - 1, ny), gz = wrap_once(z0 + lz - 1, nz);
-  const long long nynz = (long long)ny * nz, N = a.n;
-  const long long yz = (long long)gy * nz + gz;
+  const I nynz = (I)ny * nz, N = (I)a.n;
+  const I yz = (I)gy * nz + gz;
   const S* __restrict__ fo = (const S*)a.f_old;
   const float* __restrict__ F = a.force;
   const int my = ly * HZ + lz;
@@ -403,13 +405,13 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
 
   float pre[18];
   auto load = [&](int gx) {
-    const long long s = gx * nynz + yz;
+    const I s = (I)gx * nynz + yz;
 #pragma unroll
-    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(fo + p * N + s);
+    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(fo + (p * N + s));
     if (F) {
       pre[15] = F[s];
-      pre[16] = F[N + s];
-      pre[17] = F[2 * N + s];
+      pre[16] = F[(N + s)];
+      pre[17] = F[(2 * N + s)];
     } else {
       pre[15] = pre[16] = pre[17] = 0.f;
     }
@@ -453,7 +455,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       const int ra_slot = SPREAD ? (k3 == 2 ? 0 : k3 + 1) : ((k - 2) & 3);
       const int rb_slot = SPREAD ? ((k - 1) & 1) : (k3 == 0 ? 2 : k3 - 1);
       const int rc_slot = SPREAD ? 0 : (k & 1);
-      const long long s = (long long)(x0 + k - 2) * nynz + yz;
+      const I s = (I)(x0 + k - 2) * nynz + yz;
       const float* ra = ringA + ra_slot * 5 * PLANE + my;  // plane x-1: c_x = +1
       const float* rb = ringB + rb_slot * 5 * PLANE + my;  // plane x
       const float* rc = ringC + rc_slot * 5 * PLANE + my;  // plane x+1: c_x = -1
@@ -467,7 +469,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       hydro_moments(g, R, jx, jy, jz);
       S* __restrict__ fn = (S*)a.f_new;
 #pragma unroll
-      for (int p = 0; p < 15; ++p) Store<S>::st(fn + p * N + s, stored_from_dev<S>(g[p], p));
+      for (int p = 0; p < 15; ++p) Store<S>::st(fn + (p * N + s), stored_from_dev<S>(g[p], p));
       const float inv = 1.0f / (a.rho0 + R);
       a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
                                (jz + 0.5f * Fp2) * inv, R);
@@ -482,9 +484,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   }
 }
 
-template <class S, int TZ, int TY, bool SPREAD>
+template <class S, int TZ, int TY, bool SPREAD, class I>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
-  fused_slab<S, TZ, TY, SPREAD>(a, blockIdx.x, blockIdx.y, blockIdx.z,
+  fused_slab<S, TZ, TY, SPREAD, I>(a, blockIdx.x, blockIdx.y, blockIdx.z,
                                 (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
@@ -540,9 +542,9 @@ __global__ void __launch_bounds__(8 * 32 + FUSED_RING_THREADS, 2) k_ens_step(Ens
     a.spread = SlabEnds{(const EndRecord<float>*)M.ends, M.bucket_count, M.bucket_list,
                         2 * M.nsw, M.max_abs_f};
     if (M.tile == 1)
-      fused_slab<float, 16, 16, true>(a, tz, ty, tx, lt);
+      fused_slab<float, 16, 16, true, int>(a, tz, ty, tx, lt);
     else
-      fused_slab<float, 32, 8, true>(a, tz, ty, tx, lt);
+      fused_slab<float, 32, 8, true, int>(a, tz, ty, tx, lt);
     __syncthreads();
   }
 }
@@ -818,18 +820,29 @@ void lattice_init_from_hydro(Lattice* L) {
   L->f_version++;
 }
 
-template <class S, int TZ, int TY, bool SPREAD>
-static void launch_fused(Lattice* L, const FusedArgs& a) {
+template <class S, int TZ, int TY, bool SPREAD, class I>
+static void launch_fused_i(Lattice* L, const FusedArgs& a) {
   constexpr int smem = fused_smem_bytes<TZ, TY, SPREAD>();
   static bool configured = false;  // per template instance, per process
   if (!configured) {
-    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD>,
+    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     configured = true;
   }
   dim3 grid((a.nz + TZ - 1) / TZ, (a.ny + TY - 1) / TY, (a.nx + FUSED_LX - 1) / FUSED_LX);
-  k_fused_step<S, TZ, TY, SPREAD><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
+  k_fused_step<S, TZ, TY, SPREAD, I><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
   LB_CHECK_LAUNCH(1);
+}
+
+// 32-bit site indices while every offset p N + s of the 15 populations fits.
+inline bool fits_int_index(long long n) { return 15 * n < (1ll << 31); }
+
+template <class S, int TZ, int TY, bool SPREAD>
+static void launch_fused(Lattice* L, const FusedArgs& a) {
+  if (fits_int_index(a.n))
+    launch_fused_i<S, TZ, TY, SPREAD, int>(L, a);
+  else
+    launch_fused_i<S, TZ, TY, SPREAD, long long>(L, a);
 }
 
 // Pending dipole ends are spread by the step kernel itself (true), or first
