@@ -293,10 +293,12 @@ __global__ void k_f32_to_f64(const float* __restrict__ src, double* __restrict__
 // A CTA owns a TY x TZ cross-section (y, z) of FUSED_LX consecutive x planes
 // and marches along x.  For each plane it collides the cross-section plus a
 // one-site ring (TY*TZ interior threads + up to 96 ring threads) and parks
-// the post-collision values in a 4-slot ring buffer of shared memory.  Once
-// the planes x-1, x, x+1 are in the ring, each interior thread pulls its 15
+// the post-collision values in a ring buffer of shared memory.  Once the
+// planes x-1, x, x+1 are in the ring, each interior thread pulls its 15
 // post-stream populations for plane x, computes rho and u with the same force
-// used in the collision (lb.cu:286-293) and writes f(t+1), rho, u.  The next
+// used in the collision (lb.cu:286-293) and writes f(t+1), rho, u.  The three
+// populations that move only along x (0, 1, 2) come from the thread's own
+// collisions of the planes x, x-1, x+1 and stay in registers.  The next
 // plane's loads are issued before the current plane is collided.
 // ---------------------------------------------------------------------------
 constexpr int FUSED_LX = SLAB_LX;
@@ -314,24 +316,24 @@ struct FusedArgs {
   SlabEnds spread;  // pending dipole ends spread by the kernel itself (SPREAD instances)
 };
 
-// Post-collision populations wait in shared memory until the output plane can
-// pull them: those moving +x (1, 7-10) are read two planes later, those at rest
-// in x (0, 3-6) one plane later, those moving -x (2, 11-14) in the same plane.
-// With one barrier per plane that needs 4, 3 and 2 slots of 5 populations; the
+// Post-collision populations 3-14 wait in shared memory until the output plane
+// can pull them: those moving +x (7-10) are read two planes later, those at
+// rest in x (3-6) one plane later, those moving -x (11-14) in the same plane.
+// With one barrier per plane that needs 4, 3 and 2 slots of 4 populations; the
 // SPREAD instances take a second barrier per plane and need 3, 2 and 1, which
 // leaves room in shared memory for the spreading without shrinking the L1
-// cache that holds the loads in flight.
+// cache that holds the loads in flight (two CTAs of either kind fit a 132 KB
+// carveout).
 __host__ __device__ constexpr int ring_group(int p) { return cx_of(p) > 0 ? 0 : (cx_of(p) == 0 ? 1 : 2); }
-__host__ __device__ constexpr int ring_index(int p) {
-  return p == 1 || p == 0 || p == 2 ? 0 : (p <= 6 ? p - 2 : (p <= 10 ? p - 6 : p - 10));
-}
+__host__ __device__ constexpr int ring_index(int p) { return p <= 6 ? p - 3 : (p <= 10 ? p - 7 : p - 11); }
+constexpr int RING_POPS = 4;
 template <bool SPREAD>
 __host__ __device__ constexpr int ring_slots(int group) {
   return SPREAD ? 3 - group : 4 - group;
 }
 template <bool SPREAD>
 __host__ __device__ constexpr int ring_pop_planes() {
-  return 5 * (ring_slots<SPREAD>(0) + ring_slots<SPREAD>(1) + ring_slots<SPREAD>(2));
+  return RING_POPS * (ring_slots<SPREAD>(0) + ring_slots<SPREAD>(1) + ring_slots<SPREAD>(2));
 }
 
 template <int TZ, int TY>
@@ -344,6 +346,9 @@ constexpr int fused_smem_bytes() {
   return SPREAD ? SpreadLayout<TZ, TY, 1, spread_base<TZ, TY>()>::total
                 : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
+// two CTAs per SM (1 KB of each CTA's shared memory is reserved) within 132 KB
+static_assert(2 * (fused_smem_bytes<32, 8, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
+static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
 
 // One slab: tile (tz, ty, tx) of the lattice in units of (TZ, TY, FUSED_LX)
 // sites; `slab` indexes its bucket of pending ends.  Called by one CTA.
@@ -355,9 +360,10 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
   constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* ringA = reinterpret_cast<float*>(smraw);  // [NA][5][PLANE]
-  float* ringB = ringA + NA * 5 * PLANE;           // [NB][5][PLANE]
-  float* ringC = ringB + NB * 5 * PLANE;           // [NC][5][PLANE]
+  constexpr int RP = RING_POPS;
+  float* ringA = reinterpret_cast<float*>(smraw);  // [NA][RP][PLANE]
+  float* ringB = ringA + NA * RP * PLANE;          // [NB][RP][PLANE]
+  float* ringC = ringB + NB * RP * PLANE;          // [NC][RP][PLANE]
   const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int z0 = tz * TZ, y0 = ty * TY, x0 = tx * FUSED_LX;
@@ -419,6 +425,8 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   if (active) load(wrap_once(x0 - 1, nx));
 
   float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f;
+  // this site's post-collision populations 0 (plane k-1) and 1 (planes k-1, k-2)
+  float keep0 = 0.f, keep1a = 0.f, keep1b = 0.f;
   int k3 = 0;  // k % 3
   for (int k = 0; k < ex + 2; ++k) {
     float cur[18];
@@ -434,19 +442,23 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
     const int wa_slot = SPREAD ? k3 : (k & 3);
     const int wb_slot = SPREAD ? (k & 1) : k3;
     const int wc_slot = SPREAD ? 0 : (k & 1);
+    float new0 = 0.f, new1 = 0.f, new2 = 0.f;
     if (active) {
       float d[15];
 #pragma unroll
       for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>(cur[p], p);
       collide(d, cur[15], cur[16], cur[17], a.rho0, a.k, d);
-      float* wa = ringA + wa_slot * 5 * PLANE + my;
-      float* wb = ringB + wb_slot * 5 * PLANE + my;
-      float* wc = ringC + wc_slot * 5 * PLANE + my;
+      float* wa = ringA + wa_slot * RP * PLANE + my;
+      float* wb = ringB + wb_slot * RP * PLANE + my;
+      float* wc = ringC + wc_slot * RP * PLANE + my;
 #pragma unroll
-      for (int p = 0; p < 15; ++p) {
+      for (int p = 3; p < 15; ++p) {
         float* w = ring_group(p) == 0 ? wa : (ring_group(p) == 1 ? wb : wc);
         w[ring_index(p) * PLANE] = d[p];
       }
+      new0 = d[0];
+      new1 = d[1];
+      new2 = d[2];
     }
     __syncthreads();
     if (SPREAD && k + 1 < ex + 2) sp.scatter(k + 1, rt, blockDim.x);
@@ -456,12 +468,15 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       const int rb_slot = SPREAD ? ((k - 1) & 1) : (k3 == 0 ? 2 : k3 - 1);
       const int rc_slot = SPREAD ? 0 : (k & 1);
       const I s = (I)(x0 + k - 2) * nynz + yz;
-      const float* ra = ringA + ra_slot * 5 * PLANE + my;  // plane x-1: c_x = +1
-      const float* rb = ringB + rb_slot * 5 * PLANE + my;  // plane x
-      const float* rc = ringC + rc_slot * 5 * PLANE + my;  // plane x+1: c_x = -1
+      const float* ra = ringA + ra_slot * RP * PLANE + my;  // plane x-1: c_x = +1
+      const float* rb = ringB + rb_slot * RP * PLANE + my;  // plane x
+      const float* rc = ringC + rc_slot * RP * PLANE + my;  // plane x+1: c_x = -1
       float g[15];
+      g[0] = keep0;   // plane x
+      g[1] = keep1b;  // plane x-1
+      g[2] = new2;    // plane x+1, collided just now
 #pragma unroll
-      for (int p = 0; p < 15; ++p) {
+      for (int p = 3; p < 15; ++p) {
         const int off = ring_index(p) * PLANE - cy_of(p) * HZ - cz_of(p);
         g[p] = ring_group(p) == 0 ? ra[off] : (ring_group(p) == 1 ? rb[off] : rc[off]);
       }
@@ -480,6 +495,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
     Fp0 = cur[15];
     Fp1 = cur[16];
     Fp2 = cur[17];
+    keep0 = new0;
+    keep1b = keep1a;
+    keep1a = new1;
     k3 = k3 == 2 ? 0 : k3 + 1;
   }
 }

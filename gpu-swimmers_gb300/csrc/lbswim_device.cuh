@@ -419,19 +419,25 @@ __device__ __forceinline__ void stencil_axis(double x, int& x0, float& dr) {
   dr = __int_as_float(0x3f800000 + (int)m);
 }
 
-// Exponent S of the fixed-point force sums (scale 2^S) for `npending` dipole
-// ends whose largest force component is the float with bits `max_bits`: the
-// sum of all their contributions stays below 2^61 in magnitude.  Integer and
-// FP32 operations only, so every kernel that spreads derives the same S.
-__host__ __device__ inline int fixed_scale_exp(int npending, unsigned max_bits) {
+// Exponent S of the fixed-point force contributions (scale 2^S).  One
+// end-node contribution is at most w |F|: w = 1/8, the largest product of three
+// Peskin weights (each at most 1/2), when every axis has 4 or more sites, and
+// w = 1 when stencil nodes fold onto one site.  With the largest force
+// component the float with bits `max_bits`, S keeps w max|F| 2^S below 2^30, so
+// every quantised contribution fits a 32-bit integer; a site's 64-bit sum of at
+// most 16 contributions from each of fewer than 2^28 ends cannot overflow.
+// Integer and FP32 operations only, so every kernel that spreads derives the
+// same S.
+__host__ __device__ inline int fixed_scale_exp(unsigned max_bits, bool fold) {
   float m;
   memcpy(&m, &max_bits, sizeof(float));
-  if (!(m > 0.f) || npending <= 0) return 60;
-  const float b = (float)npending * m * 1.00000095367431640625f;  // 1 + 2^-20 covers rounding
+  if (!(m > 0.f)) return 30;
+  // 1 + 2^-20 covers the rounding of the weights and of this product
+  const float b = m * (fold ? 1.0f : 0.125f) * 1.00000095367431640625f;
   unsigned bb;
   memcpy(&bb, &b, sizeof(float));
   const int e = (int)((bb >> 23) & 0xffu) - 127;  // floor(log2 b) for a normal b
-  const int S = 60 - e;
+  const int S = 29 - e;                           // b 2^S < 2^(e+1) 2^S = 2^30
   return S < -100 ? -100 : (S > 100 ? 100 : S);
 }
 __host__ __device__ inline float exp2_int(int S) {  // 2^S for -126 <= S <= 127
@@ -514,11 +520,22 @@ __device__ __forceinline__ float end_contrib_f(float wy, float wz, float wxF) {
 }
 
 // ---- fixed-point force accumulation (FP32 lattices) ---------------------------
-// Each end-node contribution c = (phi_y phi_z)(phi_x F) is quantised to
-// round(c 2^S) and summed in 64-bit integers.  Integer sums are exact, so the
-// force is the same whatever order the contributions arrive in: shared-memory
-// atomics in the step kernel and the gather of k_force_tile give identical
-// bits.  The host picks S so that the sum of all |c| stays below 2^62.
+// Each end-node contribution c = (phi_y phi_z)(phi_x F) is quantised to the
+// 32-bit integer round(c 2^S) (S from fixed_scale_exp) and summed in 64-bit
+// integers.  Integer sums are exact, so the force is the same whatever order
+// the contributions arrive in: the step kernel's shared-memory atomics and the
+// force kernel give identical bits.
+__device__ __forceinline__ int fx_quant32(float c, float scale) { return __float2int_rn(c * scale); }
+// float of the 64-bit sum q * inv_scale, from its two 32-bit halves.  A sum
+// that fits 32 bits converts in one step (a small negative sum would otherwise
+// cancel between -2^32 and the rounded low half); a larger one is within two
+// float roundings.
+__device__ __forceinline__ float fx_value(long long q, float inv_scale) {
+  const int hi = (int)(q >> 32);
+  const unsigned lo = (unsigned)(q & 0xffffffffll);
+  if (hi == ((int)lo >> 31)) return __int2float_rn((int)lo) * inv_scale;
+  return (__int2float_rn(hi) * 4294967296.f + __uint2float_rn(lo)) * inv_scale;
+}
 // round(c * scale) as a 64-bit integer using only 32-bit conversions (the 64-bit
 // ones run on GB300's narrow FP64 pipe).  v = c * scale is exact (power of two);
 // when |v| >= 2^31 it is an integer with at most 24 significant bits, split
@@ -529,12 +546,6 @@ __device__ __forceinline__ long long fx_quant(float c, float scale) {
   const float hi = floorf(v * 2.3283064365386963e-10f);  // v / 2^32
   const float lo = v - hi * 4294967296.f;                 // exact, in [0, 2^32)
   return (long long)(int)hi * 4294967296ll + (long long)__float2uint_rn(lo);
-}
-// float of the 64-bit sum q * inv_scale, from its two 32-bit halves.
-__device__ __forceinline__ float fx_value(long long q, float inv_scale) {
-  const int hi = (int)(q >> 32);
-  const unsigned lo = (unsigned)(q & 0xffffffffll);
-  return (__int2float_rn(hi) * 4294967296.f + __uint2float_rn(lo)) * inv_scale;
 }
 __device__ __forceinline__ float node_contrib(float py, float pz, float wx, float F) {
   return (py * pz) * (wx * F);

@@ -445,25 +445,22 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply_total(
   }
 }
 
-// Force tile: 8 (x) x 8 (y) x 32 (z) sites, 16 warps, each warp owns 4 of the 64
-// z-rows; a warp ballot picks the ends covering a row.
-//  * FP64: the ends are put in end order by rank and every site adds their
-//    contributions in that order, ((phi_x phi_y) phi_z) F as the reference
-//    does (SwimmerArray.cu:64-73).
-//  * FP32: every end-node contribution is quantised and summed in 64-bit
-//    fixed point, exactly as the step kernel's own spreading does.
+// Force tile (FP64 lattices): 8 (x) x 8 (y) x 32 (z) sites, 16 warps, each
+// warp owns 4 of the 64 z-rows; a warp ballot picks the ends covering a row.
+// The ends are put in end order by rank and every site adds their
+// contributions in that order, ((phi_x phi_y) phi_z) F as the reference does
+// (SwimmerArray.cu:64-73).  FP32 lattices spread in the step kernel and in
+// k_force_slab instead.
 constexpr int FT_X = 8, FT_Y = 8, FT_Z = 32, FT_THREADS = 512, FT_CAP = 256;
 
-template <class T>
 __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
-                                                           const EndRecord<T>* __restrict__ ends,
+                                                           const EndRecord<double>* __restrict__ ends,
                                                            const unsigned* __restrict__ start,
                                                            const int* __restrict__ list,
                                                            int* __restrict__ sorted,
-                                                           int npending,
-                                                           const unsigned* __restrict__ max_abs_f,
-                                                           T* __restrict__ force, int accumulate) {
-  constexpr bool FIXED = sizeof(T) == 4;
+                                                           double* __restrict__ force,
+                                                           int accumulate) {
+  using T = double;
   __shared__ EndRecord<T> srec[FT_CAP];
   __shared__ int skey[FT_CAP];
   const int tile = blockIdx.x;
@@ -473,14 +470,10 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
   const int cnt = (int)(s1 - s0);
   const bool in_smem = cnt <= FT_CAP;
   if (in_smem) {
-    if (FIXED) {
-      for (int q = tid; q < cnt; q += FT_THREADS) srec[q] = ends[list[s0 + q]];
-    } else {
-      for (int q = tid; q < cnt; q += FT_THREADS) skey[q] = list[s0 + q];
-      __syncthreads();
-      for (int q = tid; q < cnt; q += FT_THREADS) srec[rank_of(skey[q], skey, cnt)] = ends[skey[q]];
-    }
-  } else if (!FIXED) {
+    for (int q = tid; q < cnt; q += FT_THREADS) skey[q] = list[s0 + q];
+    __syncthreads();
+    for (int q = tid; q < cnt; q += FT_THREADS) srec[rank_of(skey[q], skey, cnt)] = ends[skey[q]];
+  } else {
     // more ends than fit: order them in global scratch and read records from there
     for (int q = tid; q < cnt; q += FT_THREADS) {
       const int k = list[s0 + q];
@@ -490,26 +483,21 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
     }
   }
   __syncthreads();
-  auto rec = [&](int q) -> const EndRecord<T>& {
-    return in_smem ? srec[q] : ends[FIXED ? list[s0 + q] : sorted[s0 + q]];
-  };
-  const int fx_exp = FIXED ? fixed_scale_exp(npending, *max_abs_f) : 0;
-  const float fx_scale = FIXED ? exp2_int(fx_exp) : 0.f, fx_inv = FIXED ? exp2_int(-fx_exp) : 0.f;
+  auto rec = [&](int q) -> const EndRecord<T>& { return in_smem ? srec[q] : ends[sorted[s0 + q]]; };
   const int z = kz * FT_Z + lane;
   const bool zval = z < D.n[2];
   for (int row = warp; row < FT_X * FT_Y; row += FT_THREADS / 32) {
     const int x = kx * FT_X + (row >> 3), y = ky * FT_Y + (row & 7);
     if (x >= D.n[0] || y >= D.n[1]) continue;
     const long long s = (long long)x * D.n[1] * D.n[2] + (long long)y * D.n[2] + z;
-    // FP64 sums start from the base force and add the ends in end order, as
+    // the sums start from the base force and add the ends in end order, as
     // the oracle's serial spreading does
     T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-    if (!FIXED && accumulate && zval) {
+    if (accumulate && zval) {
       acc0 = force[s];
       acc1 = force[D.N + s];
       acc2 = force[2 * D.N + s];
     }
-    long long q0 = 0, q1 = 0, q2 = 0;
     bool hit = false;
     for (int base = 0; base < cnt; base += 32) {
       const int q = base + lane;
@@ -525,50 +513,26 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
         const int q2i = base + __ffs(m) - 1;
         m &= m - 1;
         const EndRecord<T>& e = rec(q2i);
-        T wx, wy, wz;
-        cover_weight(x, e.o[0], D.n[0], e.phi[0], wx);
+        T wz;
         if (!zval || !cover_weight(z, e.o[2], D.n[2], e.phi[2], wz)) continue;
         hit = true;
-        if constexpr (FIXED) {
-          // per (jy, jz) node, as the step kernel scatters them
-          for (int jy = 0; jy < 4; ++jy) {
-            if (wrap_any(e.o[1] + jy, D.n[1]) != y) continue;
-            for (int jz = 0; jz < 4; ++jz) {
-              if (wrap_any(e.o[2] + jz, D.n[2]) != z) continue;
-              const float py = e.phi[1][jy], pz = e.phi[2][jz];
-              q0 += fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-              q1 += fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-              q2 += fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
-            }
-          }
-        } else {
-          // node by node in (i, j, k) order, as AccumulateDeltaForce adds them
-          // (several nodes land on one site when an axis is shorter than 4)
-          (void)wy;
-          for (int i = 0; i < 4; ++i) {
-            if (wrap_any(e.o[0] + i, D.n[0]) != x) continue;
-            for (int j = 0; j < 4; ++j) {
-              if (wrap_any(e.o[1] + j, D.n[1]) != y) continue;
-              for (int k = 0; k < 4; ++k) {
-                if (wrap_any(e.o[2] + k, D.n[2]) != z) continue;
-                acc0 = __dadd_rn(acc0, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[0]));
-                acc1 = __dadd_rn(acc1, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[1]));
-                acc2 = __dadd_rn(acc2, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[2]));
-              }
+        // node by node in (i, j, k) order, as AccumulateDeltaForce adds them
+        // (several nodes land on one site when an axis is shorter than 4)
+        for (int i = 0; i < 4; ++i) {
+          if (wrap_any(e.o[0] + i, D.n[0]) != x) continue;
+          for (int j = 0; j < 4; ++j) {
+            if (wrap_any(e.o[1] + j, D.n[1]) != y) continue;
+            for (int k = 0; k < 4; ++k) {
+              if (wrap_any(e.o[2] + k, D.n[2]) != z) continue;
+              acc0 = __dadd_rn(acc0, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[0]));
+              acc1 = __dadd_rn(acc1, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[1]));
+              acc2 = __dadd_rn(acc2, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[2]));
             }
           }
         }
       }
     }
-    if (!zval) continue;
-    if constexpr (FIXED) {
-      // base + spread, the value the step kernel forms
-      const T b0 = accumulate ? force[s] : T(0), b1 = accumulate ? force[D.N + s] : T(0),
-              b2 = accumulate ? force[2 * D.N + s] : T(0);
-      force[s] = b0 + fx_value(q0, fx_inv);
-      force[D.N + s] = b1 + fx_value(q1, fx_inv);
-      force[2 * D.N + s] = b2 + fx_value(q2, fx_inv);
-    } else if (!accumulate || hit) {
+    if (zval && (!accumulate || hit)) {
       force[s] = acc0;
       force[D.N + s] = acc1;
       force[2 * D.N + s] = acc2;
@@ -1354,18 +1318,16 @@ static void bin_ends(Lattice* L, TileLists& TL, const TileGrid& G) {
   }
 }
 
-// Fold the pending ends into the dense force buffer (force = base + spread).
-// 2^S for the fixed-point sums of the pending ends, computed on the device.
-
-template <class T>
-static void materialise_t(Lattice* L) {
+// Fold the pending ends of an FP64 lattice into the dense force buffer
+// (force = base + spread).
+static void materialise_f64(Lattice* L) {
   SpreadScratch& S = L->spread;
   const TileGrid G = force_tiles(L);
-  bin_ends<T>(L, S.ftiles, G);
+  bin_ends<double>(L, S.ftiles, G);
   const Dims D = make_dims(L);
-  k_force_tile<T><<<S.ftiles.ntiles, FT_THREADS, 0, L->stream>>>(
-      D, G, (const EndRecord<T>*)S.ends, S.ftiles.start, S.ftiles.list, S.ftiles.sorted,
-      S.pending, S.max_abs_force, (T*)L->force, L->force_zero_pending ? 0 : 1);
+  k_force_tile<<<S.ftiles.ntiles, FT_THREADS, 0, L->stream>>>(
+      D, G, (const EndRecord<double>*)S.ends, S.ftiles.start, S.ftiles.list, S.ftiles.sorted,
+      (double*)L->force, L->force_zero_pending ? 0 : 1);
   LB_CHECK_LAUNCH(1);
   S.pending = 0;
   S.stepped = false;
@@ -1375,7 +1337,7 @@ static void materialise_t(Lattice* L) {
 void spread_materialise(Lattice* L) {
   if (L->spread.pending > 0) {
     if (L->precision == LBSWIM_F64) {
-      materialise_t<double>(L);
+      materialise_f64(L);
     } else {
       lattice_force_from_slabs(L);
       L->spread.pending = 0;

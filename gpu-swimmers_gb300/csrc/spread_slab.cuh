@@ -5,10 +5,11 @@
 // plus H sites on every side (H = 1 for the step kernel, which collides a ring
 // around its cross-section; H = 0 for the force kernel).  Its ends come from
 // the slab buckets filled when the ends were recorded.  For every local plane
-// the (end, (jy, jz) node) pairs that fall on it are added into 64-bit
-// fixed-point sums per site and component, kept as 32-bit halves so that the
-// additions are native shared-memory atomics; a sum does not depend on the
-// order of its additions, so the force is deterministic.
+// the (end, (jy, jz) node) pairs that fall on it are quantised to 32-bit
+// integers and added into 64-bit fixed-point sums per site and component, kept
+// as 32-bit halves so that the additions are native shared-memory atomics; a
+// sum does not depend on the order of its additions, so the force is
+// deterministic.
 #pragma once
 #include "lbswim_device.cuh"
 #include "lbswim_internal.h"
@@ -97,7 +98,7 @@ struct SlabSpreader {
                        int nz_, int x0_, int y0_, int z0_, int ex_, int ey_, int ez_) {
     smem = smem_;
     nx = nx_, ny = ny_, nz = nz_, x0 = x0_, y0 = y0_, z0 = z0_, ex = ex_, ey = ey_, ez = ez_;
-    const int e = fixed_scale_exp(se.npending, *se.max_abs_f);
+    const int e = fixed_scale_exp(*se.max_abs_f, nx < 4 || ny < 4 || nz < 4);
     fx_scale = exp2_int(e);
     fx_inv = exp2_int(-e);
     ends = se.ends;
@@ -187,15 +188,15 @@ struct SlabSpreader {
     }
   }
 
-  // Exact 64-bit addition into the halves: the low half's carry goes into the
-  // high half.
-  __device__ void add1(unsigned* lo, long long q) const {
+  // Exact 64-bit addition of the sign-extended q into the halves: the high
+  // half takes the sign and the low half's carry, when they do not cancel.
+  __device__ void add1(unsigned* lo, int q) const {
     const unsigned l = (unsigned)q;
     const unsigned old = atomicAdd(lo, l);
-    const int h = (int)(q >> 32) + (old + l < old ? 1 : 0);
+    const int h = (q >> 31) + (old + l < old ? 1 : 0);
     if (h != 0) atomicAdd(reinterpret_cast<int*>(lo + PLANE), h);
   }
-  __device__ void add3(int at, long long q0, long long q1, long long q2) const {
+  __device__ void add3(int at, int q0, int q1, int q2) const {
     add1(fq() + at, q0);
     add1(fq() + 2 * PLANE + at, q1);
     add1(fq() + 4 * PLANE + at, q2);
@@ -220,9 +221,9 @@ struct SlabSpreader {
         else
           wx = e.phi[0][(ent >> 8) & 3u];
         const float py = e.phi[1][jy], pz = e.phi[2][jz];
-        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+        const int q0 = fx_quant32(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+        const int q1 = fx_quant32(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+        const int q2 = fx_quant32(node_contrib(py, pz, wx, e.F[2]), fx_scale);
         if (!(ent & PL_DUP)) {
           add3(ly2 * HZ + lz2, q0, q1, q2);
         } else {
@@ -239,9 +240,9 @@ struct SlabSpreader {
         if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
         const int jy = (t >> 2) & 3, jz = t & 3;
         const float py = e.phi[1][jy], pz = e.phi[2][jz];
-        const long long q0 = fx_quant(node_contrib(py, pz, wx, e.F[0]), fx_scale);
-        const long long q1 = fx_quant(node_contrib(py, pz, wx, e.F[1]), fx_scale);
-        const long long q2 = fx_quant(node_contrib(py, pz, wx, e.F[2]), fx_scale);
+        const int q0 = fx_quant32(node_contrib(py, pz, wx, e.F[0]), fx_scale);
+        const int q1 = fx_quant32(node_contrib(py, pz, wx, e.F[1]), fx_scale);
+        const int q2 = fx_quant32(node_contrib(py, pz, wx, e.F[2]), fx_scale);
         const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
         for (int ly2 = wrap_any(yg - y0 + H, ny); ly2 <= ey - 1 + 2 * H; ly2 += ny)
           for (int lz2 = wrap_any(zg - z0 + H, nz); lz2 <= ez - 1 + 2 * H; lz2 += nz)
