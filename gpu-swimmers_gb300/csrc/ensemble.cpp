@@ -111,6 +111,15 @@ void ensemble_set_members(Ensemble* E, Lattice* const* lat, Swimmers* const* sw,
       throw LbswimError{LBSWIM_EINVAL, "ensemble members must have fewer than 143M sites"};
     for (int j = 0; j < i; ++j)
       if (lat[j] == lat[i]) throw LbswimError{LBSWIM_EINVAL, "a lattice appears twice"};
+    // the batched step keeps every slab's force sums in the split form, which
+    // holds up to 65535 contributions per site (16 per end on an axis below 4)
+    if (sw && sw[i]) {
+      const bool fold = lat[i]->size[0] < 4 || lat[i]->size[1] < 4 || lat[i]->size[2] < 4;
+      if (2ll * sw[i]->n * (fold ? 16 : 1) > 65535ll)
+        throw LbswimError{LBSWIM_EINVAL,
+                          "ensemble members take at most 32767 swimmers (2047 when an axis is "
+                          "shorter than 4 sites)"};
+    }
   }
   E->lat.assign(lat, lat + n);
   E->sw.assign(n, nullptr);

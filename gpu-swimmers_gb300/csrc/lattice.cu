@@ -354,7 +354,8 @@ static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPRE
 // sites; `slab` indexes its bucket of pending ends.  Called by one CTA.
 // I is the site-index type: int when 15 N fits it (one multiply-add per
 // address), long long otherwise.
-template <class S, int TZ, int TY, bool SPREAD, class I = long long>
+// SPLIT: the form of the slab's force sums (slab_sums_split); SPREAD only.
+template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT>
 __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
@@ -399,7 +400,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   const int my = ly * HZ + lz;
 
   // ---- this slab's pending dipole ends and the fixed-point force plane ----
-  SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>()> sp;
+  SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>(), SPLIT> sp;
   // the ring threads, which write no output plane, take the first pairs
   const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
   if (SPREAD) {
@@ -504,8 +505,11 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
 
 template <class S, int TZ, int TY, bool SPREAD, class I>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
-  fused_slab<S, TZ, TY, SPREAD, I>(a, blockIdx.x, blockIdx.y, blockIdx.z,
-                                (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+  const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  if (!SPREAD || slab_sums_split(a.spread, slab, a.nx, a.ny, a.nz))
+    fused_slab<S, TZ, TY, SPREAD, I, true>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
+  else
+    fused_slab<S, TZ, TY, SPREAD, I, false>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
 }
 
 // ---------------------------------------------------------------------------
@@ -559,10 +563,12 @@ __global__ void __launch_bounds__(8 * 32 + FUSED_RING_THREADS, 2) k_ens_step(Ens
     a.k = Relax<float>{M.omega_s, M.omega_b, M.force_s, M.force_b};
     a.spread = SlabEnds{(const EndRecord<float>*)M.ends, M.bucket_count, M.bucket_list,
                         2 * M.nsw, M.max_abs_f};
+    // members have few enough swimmers for split force sums on every slab
+    // (checked when the members are set)
     if (M.tile == 1)
-      fused_slab<float, 16, 16, true, int>(a, tz, ty, tx, lt);
+      fused_slab<float, 16, 16, true, int, true>(a, tz, ty, tx, lt);
     else
-      fused_slab<float, 32, 8, true, int>(a, tz, ty, tx, lt);
+      fused_slab<float, 32, 8, true, int, true>(a, tz, ty, tx, lt);
     __syncthreads();
   }
 }
@@ -586,16 +592,15 @@ void ens_launch_step(const EnsTable& t, int parity, int grid, cudaStream_t s) {
 // the bits are those the step kernel uses.  One thread per (y, z) site of the
 // slab's cross-section writes the three components of its site on each plane.
 // ---------------------------------------------------------------------------
-template <int TZ, int TY>
-__global__ void __launch_bounds__(TY * TZ) k_force_slab(SlabEnds se, float* __restrict__ force,
-                                                         int nx, int ny, int nz, long long N,
-                                                         int accumulate) {
+template <int TZ, int TY, bool SPLIT>
+__device__ __forceinline__ void force_slab(const SlabEnds& se, float* __restrict__ force, int nx,
+                                           int ny, int nz, long long N, int accumulate,
+                                           int slab) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int tid = threadIdx.x;
   const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY, x0 = blockIdx.z * SLAB_LX;
   const int ez = min(TZ, nz - z0), ey = min(TY, ny - y0), ex = min(SLAB_LX, nx - x0);
-  const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-  SlabSpreader<TZ, TY, 0, 0> sp;
+  SlabSpreader<TZ, TY, 0, 0, SPLIT> sp;
   sp.bind(smraw, se, slab, nx, ny, nz, x0, y0, z0, ex, ey, ez);
   sp.prologue(tid, blockDim.x);
   const int ly = tid / TZ, lz = tid % TZ;
@@ -615,6 +620,17 @@ __global__ void __launch_bounds__(TY * TZ) k_force_slab(SlabEnds se, float* __re
     }
     __syncthreads();
   }
+}
+
+template <int TZ, int TY>
+__global__ void __launch_bounds__(TY * TZ) k_force_slab(SlabEnds se, float* __restrict__ force,
+                                                         int nx, int ny, int nz, long long N,
+                                                         int accumulate) {
+  const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  if (slab_sums_split(se, slab, nx, ny, nz))
+    force_slab<TZ, TY, true>(se, force, nx, ny, nz, N, accumulate, slab);
+  else
+    force_slab<TZ, TY, false>(se, force, nx, ny, nz, N, accumulate, slab);
 }
 
 template <int TZ, int TY>

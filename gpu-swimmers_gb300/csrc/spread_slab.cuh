@@ -6,10 +6,13 @@
 // around its cross-section; H = 0 for the force kernel).  Its ends come from
 // the slab buckets filled when the ends were recorded.  For every local plane
 // the (end, (jy, jz) node) pairs that fall on it are quantised to 32-bit
-// integers and added into 64-bit fixed-point sums per site and component, kept
-// as 32-bit halves so that the additions are native shared-memory atomics; a
+// integers and added into exact integer sums per site and component, kept as
+// two 32-bit words so that the additions are native shared-memory atomics; a
 // sum does not depend on the order of its additions, so the force is
-// deterministic.
+// deterministic.  While a site can take at most 65535 contributions (the usual
+// case) a contribution q goes in as its low 16 bits (unsigned) and q >> 16 with
+// two atomics that return nothing; otherwise as a 64-bit sum whose high word
+// takes the carries of the low one.
 #pragma once
 #include "lbswim_device.cuh"
 #include "lbswim_internal.h"
@@ -45,7 +48,7 @@ __device__ __forceinline__ int wrap_small(int i, int n) {
 }
 
 // Byte offsets of the spreading state from byte BASE of shared memory:
-// fixed-point sums of one plane [3][lo, hi][PLANE], coverage masks [CAP] (u64),
+// fixed-point sums of one plane [3][PLANE][2 words], coverage masks [CAP] (u64),
 // ends [CAP], local node rows [CAP], per-plane list offsets [LX + 2H + 1],
 // plane lists [CAP * SPREAD_PLANES_PER_END] (u16).
 template <int TZ, int TY, int H, int BASE>
@@ -70,7 +73,22 @@ struct SlabEnds {
   const unsigned* max_abs_f;
 };
 
-template <int TZ, int TY, int H, int BASE>
+// Whether the sums of slab `slab` can take the split form: a site takes at
+// most one contribution per end of the slab (16 when stencil nodes fold onto
+// one site), and 65535 contributions keep the sum of their low 16 bits below
+// 2^32.  Every spreader of the slab, and the code that reads its sums, makes
+// the same choice.
+__device__ __forceinline__ bool slab_sums_split(const SlabEnds& se, int slab, int nx, int ny,
+                                                int nz) {
+  const unsigned c = se.count[slab];
+  const long long cnt = c > (unsigned)SLAB_BUCKET_CAP ? se.npending : (long long)c;
+  return cnt * (nx < 4 || ny < 4 || nz < 4 ? 16 : 1) <= 65535ll;
+}
+
+// SPLIT: the sums are (sum of the low 16 bits, sum of q >> 16), each added
+// with an atomic that returns nothing; otherwise 64-bit sums whose high word
+// takes the low word's carries (slab_sums_split decides).
+template <int TZ, int TY, int H, int BASE, bool SPLIT>
 struct SlabSpreader {
   static constexpr int HZ = TZ + 2 * H, PLANE = (TY + 2 * H) * HZ;
   using SL = SpreadLayout<TZ, TY, H, BASE>;
@@ -188,18 +206,25 @@ struct SlabSpreader {
     }
   }
 
-  // Exact 64-bit addition of the sign-extended q into the halves: the high
-  // half takes the sign and the low half's carry, when they do not cancel.
-  __device__ void add1(unsigned* lo, int q) const {
-    const unsigned l = (unsigned)q;
-    const unsigned old = atomicAdd(lo, l);
-    const int h = (q >> 31) + (old + l < old ? 1 : 0);
-    if (h != 0) atomicAdd(reinterpret_cast<int*>(lo + PLANE), h);
+  // Exact addition of q into the two words w[0], w[1] of a sum.  Split: the
+  // low 16 bits (at most 65535 of them sum below 2^32) and q >> 16 (their sum
+  // stays within 32 bits).  Otherwise a 64-bit sum: the high word takes the
+  // sign of q and the low word's carry, when they do not cancel.
+  __device__ void add1(unsigned* w, int q) const {
+    if (SPLIT) {
+      atomicAdd(w, (unsigned)q & 0xffffu);
+      atomicAdd(reinterpret_cast<int*>(w + 1), q >> 16);
+    } else {
+      const unsigned l = (unsigned)q;
+      const unsigned old = atomicAdd(w, l);
+      const int h = (q >> 31) + (old + l < old ? 1 : 0);
+      if (h != 0) atomicAdd(reinterpret_cast<int*>(w + 1), h);
+    }
   }
   __device__ void add3(int at, int q0, int q1, int q2) const {
-    add1(fq() + at, q0);
-    add1(fq() + 2 * PLANE + at, q1);
-    add1(fq() + 4 * PLANE + at, q2);
+    add1(fq() + 2 * at, q0);
+    add1(fq() + 2 * (PLANE + at), q1);
+    add1(fq() + 2 * (2 * PLANE + at), q2);
   }
 
   // Add the contributions of local plane kk; this thread takes the pairs
@@ -229,7 +254,8 @@ struct SlabSpreader {
         } else {
           // tiny lattice: a node can appear at several places of the cross-section
           for (int a2 = ly2; a2 <= ey - 1 + 2 * H; a2 += ny)
-            for (int b2 = lz2; b2 <= ez - 1 + 2 * H; b2 += nz) add3(a2 * HZ + b2, q0, q1, q2);
+            for (int b2 = lz2; b2 <= ez - 1 + 2 * H; b2 += nz)
+              add3(a2 * HZ + b2, q0, q1, q2);
         }
       }
     } else {
@@ -253,9 +279,11 @@ struct SlabSpreader {
 
   // The sum of component c at local site `at` as a float, and zero it.
   __device__ float take(int at, int c) const {
-    unsigned* lo = fq() + 2 * c * PLANE + at;
-    const long long q = (long long)(((unsigned long long)lo[PLANE] << 32) | lo[0]);
-    lo[0] = lo[PLANE] = 0u;
+    uint2* p = reinterpret_cast<uint2*>(fq()) + c * PLANE + at;
+    const uint2 w = *p;
+    *p = make_uint2(0u, 0u);
+    const long long q = SPLIT ? (long long)(int)w.y * 65536ll + (long long)w.x
+                              : (long long)(((unsigned long long)w.y << 32) | w.x);
     return fx_value(q, fx_inv);
   }
 };

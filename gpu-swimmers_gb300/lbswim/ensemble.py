@@ -32,7 +32,9 @@ class Ensemble:
 
     def set_members(self, members):
         """Replace the membership by a list of (lattice, swimmers or None,
-        tracers or None); the objects must stay alive while they are members."""
+        tracers or None); the objects must stay alive while they are members.
+        A member's swimmer array holds at most 32767 swimmers (2047 when an
+        axis of its lattice is shorter than 4 sites)."""
         members = [tuple(m) + (None,) * (3 - len(m)) for m in members]
         n = len(members)
         arr = C.c_void_p * max(n, 1)

@@ -274,8 +274,11 @@ int lbswim_lattice_set_tau(lbswim_lattice* lat, double tau_s, double tau_b);
  * graph.  Each member ends exactly where lbswim_system_step would have taken
  * it (bit for bit, with the same slab shape).  Membership can change between
  * calls to lbswim_ensemble_step; members stay owned by the caller and must
- * outlive their membership.  autotune picks, per lattice shape, the slab shape
- * that runs fastest (timed on scratch copies; results cached per shape). */
+ * outlive their membership.  A member lattice has fewer than 143M sites and its
+ * swimmer array at most 32767 swimmers (2047 when an axis is shorter than 4
+ * sites); set_members returns LBSWIM_EINVAL otherwise.  autotune picks, per
+ * lattice shape, the slab shape that runs fastest (timed on scratch copies;
+ * results cached per shape). */
 typedef struct lbswim_ensemble lbswim_ensemble;
 int lbswim_ensemble_create(lbswim_ensemble** out);
 int lbswim_ensemble_destroy(lbswim_ensemble* ens);

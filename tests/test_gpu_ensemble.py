@@ -98,3 +98,21 @@ def test_fp32_ensemble_velocity_within_1e5_of_fp64():
         gs, rs = snapshot(*b[:3]), snapshot(*ref[:3])
         assert rel_l2(gs["u"], rs["u"]) < 1e-5
         assert rel_l2(gs["rho"], rs["rho"]) < 1e-6
+
+
+def test_member_swimmer_limit():
+    # a member takes at most 32767 swimmers (2047 on a lattice with an axis
+    # shorter than 4 sites): beyond that its force sums could leave the split form
+    from lbswim import _lib, lb, swimmers
+    from lbswim.ensemble import Ensemble
+    ens = Ensemble()
+    for size, ok, bad in (((8, 8, 8), 32767, 32768), ((3, 8, 8), 2047, 2048)):
+        lat = lb.Lattice(*size, 0.8, 0.8, precision="f32")
+        for n, fine in ((ok, True), (bad, False)):
+            sw = swimmers.Array(n, swimmers.CommonParams())
+            if fine:
+                ens.set_members([(lat, sw)])
+                ens.set_members([])
+            else:
+                with pytest.raises(_lib.LbswimError, match="32767 swimmers"):
+                    ens.set_members([(lat, sw)])

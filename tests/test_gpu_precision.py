@@ -58,14 +58,18 @@ def _spread_case():
     return O.random_case((40, 24, 36), 400, 300, seed=21, alpha=0.1, P=2e-3, l=0.4)
 
 
-@pytest.mark.parametrize("dense", [False, True])
-def test_f32_in_kernel_spread_equals_materialised_force(dense):
+@pytest.mark.parametrize("kind", ["sparse", "dense", "folded"])
+def test_f32_in_kernel_spread_equals_materialised_force(kind):
     # (a) the step kernel spreads the pending ends itself; (b) the force is read
     # back first, which writes the dense field, and the step then reads it.
     # The dense case puts more ends on one slab and one plane than the kernel's
-    # shared-memory lists hold, which exercises its fallbacks.
-    case = (O.random_case((16, 16, 16), 600, 50, seed=3, alpha=0.1, P=2e-3, l=0.4) if dense
-            else _spread_case())
+    # shared-memory lists hold, which exercises its fallbacks; the folded case
+    # also takes the 64-bit sums with carries.
+    case = {"sparse": _spread_case,
+            "dense": lambda: O.random_case((16, 16, 16), 600, 50, seed=3, alpha=0.1, P=2e-3,
+                                           l=0.4),
+            "folded": lambda: O.random_case((3, 8, 12), 2100, 10, seed=5, alpha=0.1, P=2e-3,
+                                            l=0.4)}[kind]()
     a = build_gpu(case, "f32")
     b = build_gpu(case, "f32")
     for t in range(6):
@@ -83,8 +87,13 @@ def test_f32_in_kernel_spread_equals_materialised_force(dense):
         assert np.array_equal(sa[k], sb[k]), k
 
 
-def test_f32_force_matches_f64_force():
-    case = _spread_case()
+@pytest.mark.parametrize("folded", [False, True])
+def test_f32_force_matches_f64_force(folded):
+    # folded: an axis of 3 sites folds stencil nodes onto one site, and 4200
+    # ends on every slab can put more than 65535 contributions on a site, so the
+    # sums take their 64-bit form with carries
+    case = (O.random_case((3, 8, 12), 2100, 10, seed=5, alpha=0.1, P=2e-3, l=0.4) if folded
+            else _spread_case())
     l32 = build_gpu(case, "f32")
     l64 = build_gpu(case, "f64")
     for lat, sw, _, _ in (l32, l64):
