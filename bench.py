@@ -271,6 +271,8 @@ def config_dict(args, world):
                         "distributions" % (args.size, nsw, ntr, args.precision),
             "lattice": [args.size] * 3, "swimmers": nsw, "tracers": ntr, "tau": 0.8,
             "precision": args.precision, "parallelism": "replicas x%d" % world,
+            "streams": "lattice on a highest-priority stream (lbswim_lattice_set_stream), "
+                       "tracer moves on their own least-priority stream",
             "l2": "no flush: each step streams %.2f GB of distributions, larger than the "
                   "129 MB L2" % (2 * 15 * args.size ** 3 * {"f64": 8, "f32": 4}.get(
                       args.precision, 2) / 1e9)}
@@ -299,8 +301,13 @@ def our_arm(args, world, rank, local):
     case = workload((side, side, side), nsw, ntr, seed=42 + rank)
     N = side ** 3
     lat, sw, tr, system = build_objects(case, args.precision)
+    # The lattice (and the particles moved with it) on a stream of the highest
+    # priority: the step kernels are dispatched ahead of tracer blocks still
+    # queued on the tracers' own least-priority stream, which fill the SMs the
+    # step leaves idle.
+    stream = torch.cuda.Stream(priority=-5)
+    lat.set_stream(stream.cuda_stream)
     upload(case, lat, sw, tr)
-    stream = torch.cuda.default_stream()  # the library launches on the legacy default stream
 
     def barrier():
         torch.cuda.synchronize()

@@ -1642,7 +1642,12 @@ void tracers_move(Tracers* T, Lattice* L) {
 void tracers_move_async(Tracers* T, Lattice* L) {
   if (T->n <= 0) return;
   if (!T->side) {
-    LB_CUDA(cudaStreamCreateWithFlags(&T->side, cudaStreamNonBlocking));
+    // Least priority: when the lattice's stream has a higher one, the next
+    // step's blocks are dispatched ahead of tracer blocks still queued, and the
+    // tracer move fills the SMs the step leaves idle.
+    int least = 0, greatest = 0;
+    LB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    LB_CUDA(cudaStreamCreateWithPriority(&T->side, cudaStreamNonBlocking, least));
     LB_CUDA(cudaEventCreateWithFlags(&T->done, cudaEventDisableTiming));
   }
   LB_CUDA(cudaStreamWaitEvent(T->side, L->hydro_ready, 0));
