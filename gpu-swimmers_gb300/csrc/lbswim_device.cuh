@@ -216,6 +216,23 @@ __device__ __forceinline__ T peskin_delta(T x) {
   }
   return T(0.125) * phi;
 }
+// The four weights phi(dr - j), j = 0..3, of a stencil whose origin is
+// ceil(x - 2), so that 1 <= dr <= 2 (FP32 paths).  With a = dr - 1 the four
+// distances are 1 + a, a, 1 - a and 2 - a; both branches of the delta above
+// then take the same square root, s = sqrt(1 + 4a(1 - a)), and
+// phi = (3 - 2a - s, 3 - 2a + s, 1 + 2a + s, 1 + 2a - s) / 8: one square root
+// for the four weights, which sum to one up to rounding.  Each weight is at
+// most 1/2, as the delta's.
+__device__ __forceinline__ void peskin_weights4(float dr, float w[4]) {
+  const float a = dr - 1.f;  // exact for 1 <= dr <= 2
+  const float s = sqrtf(fmaf(4.f * a, 1.f - a, 1.f));
+  const float p = 3.f - 2.f * a, q = 1.f + 2.f * a;
+  w[0] = 0.125f * (p - s);
+  w[1] = 0.125f * (p + s);
+  w[2] = 0.125f * (q + s);
+  w[3] = 0.125f * (q - s);
+}
+
 // FP64: the reference's operations in its order, each rounded on its own (no
 // fused multiply-add), so that FP64 lattices can reproduce the oracle bit for bit.
 template <>

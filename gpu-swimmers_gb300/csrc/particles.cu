@@ -320,7 +320,8 @@ __device__ __forceinline__ void bucket_end(int e, const int o[3], const Dims& D,
 // bucket_count set, each end is also listed under the step-kernel slabs it
 // touches (its index among all pending ends is e_base + e).  FP32 records take
 // the stencil origin from the bits of the position (stencil_axis) and the
-// weights of dr - i, like the FP32 interpolation.
+// four weights from one square root (peskin_weights4), like the FP32
+// interpolation.
 template <class T>
 __device__ __forceinline__ void end_records_block(
     int blk, int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P,
@@ -351,8 +352,10 @@ __device__ __forceinline__ void end_records_block(
         float dr;
         stencil_axis(rr[a], x0, dr);
         rec.o[a] = wrap_any(x0, D.n[a]);
+        float w[4];
+        peskin_weights4(dr, w);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) rec.phi[a][j] = peskin_delta<float>(dr - (float)j);
+        for (int j = 0; j < 4; ++j) rec.phi[a][j] = w[j];
       }
     } else {
       stencil_setup<T>(D, rr, rec.o, rec.phi);
@@ -551,7 +554,8 @@ __device__ __forceinline__ void interp_setup(const Dims& D, const double r[3], i
   for (int d = 0; d < 3; ++d) {
     const double x0 = ceil(r[d] - 2.);
     const int o = wrap_any((int)x0, D.n[d]);
-    const float dr = (float)(r[d] - x0);
+    float w[4];
+    if constexpr (sizeof(T) == 4) peskin_weights4((float)(r[d] - x0), w);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int t = o + i;
@@ -560,7 +564,7 @@ __device__ __forceinline__ void interp_setup(const Dims& D, const double r[3], i
       if constexpr (sizeof(T) == 8)
         phi[d][i] = peskin_delta<T>(r[d] - (x0 + i));
       else
-        phi[d][i] = peskin_delta<T>(dr - (float)i);
+        phi[d][i] = w[i];
     }
   }
 }
@@ -898,9 +902,12 @@ __device__ __forceinline__ void point_stencil(const Dims& D, const double r[3],
   }
   st.active[p] = 1;
 #pragma unroll
-  for (int j = 0; j < 4; ++j)
+  for (int d = 0; d < 3; ++d) {
+    float w[4];
+    peskin_weights4(dr[d], w);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) st.w[d][j][p] = peskin_delta<float>(dr[d] - (float)j);
+    for (int j = 0; j < 4; ++j) st.w[d][j][p] = w[j];
+  }
 }
 
 __device__ __forceinline__ int node_after(int o, int j, int n) {
