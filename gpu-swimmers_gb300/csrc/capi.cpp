@@ -54,6 +54,20 @@ int lbswim_kernel_launches(unsigned long long* count) {
   return LBSWIM_OK;
 }
 
+int lbswim_host_alloc(size_t bytes, void** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  LB_CUDA(cudaMallocHost(out, bytes ? bytes : 16));
+  API_END
+}
+
+int lbswim_host_free(void* ptr) {
+  API_BEGIN
+  if (ptr) LB_CUDA(cudaFreeHost(ptr));
+  API_END
+}
+
 // ---- Lattice -------------------------------------------------------------------
 int lbswim_lattice_create(int nx, int ny, int nz, double tau_s, double tau_b, int precision,
                           lbswim_lattice** out) {
@@ -320,6 +334,7 @@ int lbswim_swimmers_destroy(lbswim_swimmers* sw) {
   cudaFree(W->r);
   cudaFree(W->v);
   cudaFree(W->nv);
+  if (W->done) cudaEventDestroy(W->done);
   delete W;
   API_END
 }
@@ -371,7 +386,9 @@ int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host) {
   API_BEGIN
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
-  LB_CUDA(cudaDeviceSynchronize());  // particle arrays are not bound to one stream
+  // the arrays are not bound to one stream: wait for the last kernel that used
+  // them (on whichever stream), not for the whole device
+  swimmers_wait(W);
   LB_CUDA(cudaMemcpy(sw_field(W, field), host, sizeof(double) * 3 * W->n, cudaMemcpyHostToDevice));
   API_END
 }
@@ -380,7 +397,7 @@ int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host) {
   API_BEGIN
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
-  LB_CUDA(cudaDeviceSynchronize());
+  swimmers_wait(W);
   LB_CUDA(cudaMemcpy(host, sw_field(W, field), sizeof(double) * 3 * W->n, cudaMemcpyDeviceToHost));
   API_END
 }

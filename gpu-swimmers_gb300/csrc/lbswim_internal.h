@@ -133,6 +133,9 @@ struct Swimmers {
   double* r = nullptr;
   double* v = nullptr;
   double* nv = nullptr;
+  // recorded on the stream of the last kernel that read or wrote the arrays,
+  // so that host copies wait for that work only (not for other streams)
+  cudaEvent_t done = nullptr;
 };
 
 // Tracers live on the device in a work order binned by position (8^3-site
@@ -274,6 +277,8 @@ void spread_free(SpreadScratch& S);
 // particles.cu
 void swimmers_add_forces(Swimmers* S, Lattice* L);
 void swimmers_move(Swimmers* S, Lattice* L);
+// Wait on the host for the last kernel that used the swimmer arrays.
+void swimmers_wait(Swimmers* S);
 void tracers_move(Tracers* T, Lattice* L);
 // Move on the tracers' own stream after the point of the lattice stream where
 // L->hydro_ready was last recorded.

@@ -1442,6 +1442,15 @@ static void append_ends_t(Swimmers* W, Lattice* L) {
   S.pending += nends;
 }
 
+static void swimmers_mark(Swimmers* W, cudaStream_t stream) {
+  if (!W->done) LB_CUDA(cudaEventCreateWithFlags(&W->done, cudaEventDisableTiming));
+  LB_CUDA(cudaEventRecord(W->done, stream));
+}
+
+void swimmers_wait(Swimmers* W) {
+  if (W->done) LB_CUDA(cudaEventSynchronize(W->done));
+}
+
 // SwimmerArray::AddForces (SwimmerArray.cu:114-121).
 void swimmers_add_forces(Swimmers* W, Lattice* L) {
   // ends already spread by a Step belong to the base from now on
@@ -1452,6 +1461,7 @@ void swimmers_add_forces(Swimmers* W, Lattice* L) {
   } else {
     append_ends_t<float>(W, L);
   }
+  swimmers_mark(W, L->stream);
   L->force_version++;
 }
 
@@ -1470,6 +1480,7 @@ void swimmers_move(Swimmers* W, Lattice* L) {
                             SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     LB_CHECK_LAUNCH(1);
+    swimmers_mark(W, L->stream);
   }
   W->step++;
 }

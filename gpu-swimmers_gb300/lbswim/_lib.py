@@ -7,6 +7,8 @@ raises ImportError.
 import ctypes as C
 import os
 
+import numpy as np
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_liblbswim.so")
 
@@ -57,6 +59,8 @@ _PROTOS = {
     "lbswim_last_error": (C.c_char_p, []),
     "lbswim_version": (C.c_char_p, []),
     "lbswim_kernel_launches": (C.c_int, [C.POINTER(C.c_ulonglong)]),
+    "lbswim_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_VP)]),
+    "lbswim_host_free": (C.c_int, [_VP]),
     "lbswim_lattice_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_int, C.POINTER(_VP)]),
     "lbswim_lattice_destroy": (C.c_int, [_VP]),
@@ -146,6 +150,34 @@ def dptr(a):
     if a.dtype.char != "d" or not a.flags.c_contiguous:
         raise TypeError("expected a C-contiguous float64 array")
     return a.ctypes.data_as(_D)
+
+
+class _PinnedBlock:
+    """Page-locked host memory from lbswim_host_alloc, freed with the block."""
+
+    def __init__(self, nbytes):
+        self.ptr = _VP()
+        check(lib.lbswim_host_alloc(max(int(nbytes), 8), C.byref(self.ptr)))
+
+    def __del__(self):
+        ptr, self.ptr = getattr(self, "ptr", None), None
+        if ptr and lib is not None:
+            try:
+                lib.lbswim_host_free(ptr)
+            except Exception:
+                pass
+
+
+def pinned_zeros(n):
+    """A zeroed float64 numpy array of n elements in page-locked host memory.
+    The memory lives as long as any array or view made from it."""
+    n = int(n)
+    block = _PinnedBlock(8 * n)
+    cbuf = (C.c_double * max(n, 1)).from_address(block.ptr.value)
+    cbuf._block = block  # views of the array keep cbuf, and cbuf the block
+    a = np.ctypeslib.as_array(cbuf)[:n]
+    a[:] = 0.0
+    return a
 
 
 def kernel_launches():

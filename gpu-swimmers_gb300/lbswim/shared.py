@@ -13,11 +13,14 @@ from . import _lib
 class Array:
     """Host copy of a device array (shared.pyx:6-35)."""
 
-    def __init__(self, owner, size, h2d, d2h):
+    def __init__(self, owner, size, h2d, d2h, pinned=False):
+        """pinned: hold the host copy in page-locked memory (particle arrays,
+        which are copied every step in typical loops)."""
         self.owner = owner
         self._h2d = h2d
         self._d2h = d2h
-        self.view = np.zeros(int(size), dtype=np.float64)
+        self.view = (_lib.pinned_zeros(size) if pinned
+                     else np.zeros(int(size), dtype=np.float64))
 
     def init(self, owner, sa):  # reference-style construction hook
         return self

@@ -27,7 +27,7 @@ class Array:
         def d2h(buf):
             _lib.check(_lib.lib.lbswim_tracers_d2h(h, which, _lib.dptr(buf)))
 
-        a = shared.Array(self, 3 * self.num, h2d, d2h)
+        a = shared.Array(self, 3 * self.num, h2d, d2h, pinned=True)
         a.view = a.view.reshape(3, self.num)
         return a
 

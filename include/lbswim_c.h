@@ -121,6 +121,11 @@ const char* lbswim_last_error(void);
 const char* lbswim_version(void);
 /* Number of this library's kernels launched so far in this process. */
 int lbswim_kernel_launches(unsigned long long* count);
+/* No reference counterpart: page-locked host memory (cudaMallocHost) for the
+ * host copies of particle arrays, which *_h2d / *_d2h then move at the link's
+ * full rate instead of through a staging copy.  host_free takes NULL. */
+int lbswim_host_alloc(size_t bytes, void** out);
+int lbswim_host_free(void* ptr);
 
 /* ---- Lattice (lb.cu, Lattice.h) ------------------------------------------- */
 /* Lattice::Lattice(nx, ny, nz, tau_s, tau_b), lb.cu:40-63.  precision selects
