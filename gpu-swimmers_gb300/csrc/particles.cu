@@ -264,7 +264,9 @@ struct TileGrid {
 // the sites o-h .. o+3+h form one cyclic interval, so the tiles form the cyclic
 // range first, first+1, ... (count of them, at most nt).  An interval that
 // wraps past the end covers the tiles from `first` to the last one and from 0
-// to the tile of its wrapped end; if those meet, it covers every tile.
+// to the tile of its wrapped end; if those meet, it covers every tile.  o is a
+// wrapped node (0 <= o < n, as records hold them) and h < n; the tile edge T
+// is a power of two (slab and force-tile shapes all are), so tiles are shifts.
 __device__ __forceinline__ void touched_range(int o, int n, int T, int h, int nt, int& first,
                                               int& count) {
   const int len = 4 + 2 * h;
@@ -273,12 +275,13 @@ __device__ __forceinline__ void touched_range(int o, int n, int T, int h, int nt
     count = nt;
     return;
   }
-  const int a = wrap_any(o - h, n), b = a + len - 1;
-  first = a / T;
+  const int sh = __ffs(T) - 1;
+  const int a = o - h < 0 ? o - h + n : o - h, b = a + len - 1;
+  first = a >> sh;
   if (b < n) {
-    count = b / T - first + 1;
+    count = (b >> sh) - first + 1;
   } else {
-    const int last = (b - n) / T;
+    const int last = (b - n) >> sh;
     count = last >= first ? nt : (nt - first) + last + 1;
   }
 }
@@ -455,6 +458,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply_total(
 // (SwimmerArray.cu:64-73).  FP32 lattices spread in the step kernel and in
 // k_force_slab instead.
 constexpr int FT_X = 8, FT_Y = 8, FT_Z = 32, FT_THREADS = 512, FT_CAP = 256;
+static_assert((FT_X & (FT_X - 1)) == 0 && (FT_Y & (FT_Y - 1)) == 0 && (FT_Z & (FT_Z - 1)) == 0,
+              "tile edges are powers of two (touched_range shifts)");
 
 __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
                                                            const EndRecord<double>* __restrict__ ends,

@@ -298,7 +298,11 @@ class Lattice:
             def d2h(buf, which=which):
                 _lib.check(_lib.lib.lbswim_lattice_d2h(h, which, _lib.dptr(buf)))
 
-            f = SharedLatticeArray(self, shared.Array(self, n, h2d, d2h))
+            # rho, u and force (the fields a host loop reads and writes) keep
+            # their host copy in page-locked memory up to 2 GB per field
+            pinned = (which in (_lib.FIELD_RHO, _lib.FIELD_U, _lib.FIELD_FORCE)
+                      and 8 * n <= (1 << 31))
+            f = SharedLatticeArray(self, shared.Array(self, n, h2d, d2h, pinned=pinned))
             self._fields[which] = f
         return f
 

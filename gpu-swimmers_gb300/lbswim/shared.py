@@ -19,8 +19,14 @@ class Array:
         self.owner = owner
         self._h2d = h2d
         self._d2h = d2h
-        self.view = (_lib.pinned_zeros(size) if pinned
-                     else np.zeros(int(size), dtype=np.float64))
+        self.view = None
+        if pinned:
+            try:
+                self.view = _lib.pinned_zeros(size)
+            except _lib.LbswimError:  # no page-locked memory left: pageable
+                self.view = None
+        if self.view is None:
+            self.view = np.zeros(int(size), dtype=np.float64)
 
     def init(self, owner, sa):  # reference-style construction hook
         return self
