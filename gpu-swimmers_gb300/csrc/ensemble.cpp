@@ -107,7 +107,7 @@ void ensemble_set_members(Ensemble* E, Lattice* const* lat, Swimmers* const* sw,
     if (!lat[i]) throw LbswimError{LBSWIM_EINVAL, "ensemble member lattice is NULL"};
     if (lat[i]->precision != LBSWIM_F32)
       throw LbswimError{LBSWIM_EINVAL, "ensemble members must be FP32 lattices"};
-    if (15 * lat[i]->n >= (1ll << 31))
+    if (15 * f_sites(lat[i]->n, LBSWIM_F32) >= (1ll << 31))
       throw LbswimError{LBSWIM_EINVAL, "ensemble members must have fewer than 143M sites"};
     for (int j = 0; j < i; ++j)
       if (lat[j] == lat[i]) throw LbswimError{LBSWIM_EINVAL, "a lattice appears twice"};

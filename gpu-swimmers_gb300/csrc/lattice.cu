@@ -167,7 +167,7 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
        s += (long long)gridDim.x * blockDim.x) {
     T d[15];
 #pragma unroll
-    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((T)Store<S>::ld(f + p * N + s), p);
+    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((T)Store<S>::ld(f + fidx<S>(p, s, N)), p);
     T R, jx, jy, jz;
     hydro_moments(d, R, jx, jy, jz);
     T fx, fy, fz;
@@ -207,7 +207,7 @@ __global__ void k_init_from_hydro(const double* __restrict__ rho, const double* 
     project<double>(r - rho0, r * ux, r * uy, r * uz, r * ux * ux, r * uy * uy, r * uz * uz,
                     r * ux * uy, compat_sxz ? r * ux * uy : r * ux * uz, r * uy * uz, out);
 #pragma unroll
-    for (int p = 0; p < 15; ++p) Store<S>::st(f + p * N + s, stored_from_dev<S>(out[p], p));
+    for (int p = 0; p < 15; ++p) Store<S>::st(f + fidx<S>(p, s, N), stored_from_dev<S>(out[p], p));
   }
 }
 
@@ -220,7 +220,7 @@ __global__ void k_calc_hydro_packed(const S* __restrict__ f, const float* __rest
        s += (long long)gridDim.x * blockDim.x) {
     float d[15];
 #pragma unroll
-    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((float)Store<S>::ld(f + p * N + s), p);
+    for (int p = 0; p < 15; ++p) d[p] = dev_from_stored<S>((float)Store<S>::ld(f + fidx<S>(p, s, N)), p);
     float R, jx, jy, jz;
     hydro_moments(d, R, jx, jy, jz);
     float fx, fy, fz;
@@ -254,7 +254,9 @@ __global__ void k_packed_to_f64(const float* __restrict__ packed, double* __rest
   }
 }
 
-// Host FP64 <-> device storage conversions for H2D / D2H of fOld and fNew.
+// Host FP64 <-> device storage conversions for H2D / D2H of fOld and fNew:
+// host element e of the reference's [15][N] order is population e / N at site
+// e % N, stored at fidx.
 template <class S>
 __global__ void k_f_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long off,
                              long long cnt, long long N, double rho0) {
@@ -263,7 +265,7 @@ __global__ void k_f_from_f64(const double* __restrict__ src, S* __restrict__ dst
     const long long e = off + i;
     const int p = (int)(e / N);
     const double d = src[i] - w_of(p) * rho0;
-    Store<S>::st(dst + e, (S)stored_from_dev<S>(d, p));
+    Store<S>::st(dst + fidx<S>(p, e - p * N, N), (S)stored_from_dev<S>(d, p));
   }
 }
 template <class S>
@@ -273,7 +275,8 @@ __global__ void k_f_to_f64(const S* __restrict__ src, double* __restrict__ dst, 
        i += (long long)gridDim.x * blockDim.x) {
     const long long e = off + i;
     const int p = (int)(e / N);
-    dst[i] = dev_from_stored<S>((double)Store<S>::ld(src + e), p) + w_of(p) * rho0;
+    dst[i] = dev_from_stored<S>((double)Store<S>::ld(src + fidx<S>(p, e - p * N, N)), p) +
+             w_of(p) * rho0;
   }
 }
 __global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long cnt) {
@@ -357,6 +360,7 @@ static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPRE
 // SPLIT: the form of the slab's force sums (slab_sums_split); SPREAD only.
 template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT>
 __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
+  static_assert(sizeof(S) < 8, "the fused step serves the reduced-precision layouts");
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
   constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
@@ -414,7 +418,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   auto load = [&](int gx) {
     const I s = (I)gx * nynz + yz;
 #pragma unroll
-    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(fo + (p * N + s));
+    const S* __restrict__ b = fo + fidx<S, I>(0, s, N);
+#pragma unroll
+    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(b + p * 32);
     if (F) {
       pre[15] = F[s];
       pre[16] = F[(N + s)];
@@ -485,7 +491,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       hydro_moments(g, R, jx, jy, jz);
       S* __restrict__ fn = (S*)a.f_new;
 #pragma unroll
-      for (int p = 0; p < 15; ++p) Store<S>::st(fn + (p * N + s), stored_from_dev<S>(g[p], p));
+      S* __restrict__ bo = fn + fidx<S, I>(0, s, N);
+#pragma unroll
+      for (int p = 0; p < 15; ++p) Store<S>::st(bo + p * 32, stored_from_dev<S>(g[p], p));
       const float inv = 1.0f / (a.rho0 + R);
       a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
                                (jz + 0.5f * Fp2) * inv, R);
@@ -676,8 +684,9 @@ void lattice_alloc(Lattice* L) {
   const long long N = L->n;
   const size_t fe = elem_bytes(L->precision);
   const size_t he = L->precision == LBSWIM_F64 ? 8 : 4;
-  L->f[0] = dmalloc(15 * N * fe);
-  L->f[1] = dmalloc(15 * N * fe);
+  const size_t fbytes = 15 * f_sites(N, L->precision) * fe;
+  L->f[0] = dmalloc(fbytes);
+  L->f[1] = dmalloc(fbytes);
   if (L->precision == LBSWIM_F64) {
     L->rho = dmalloc(N * he);
     L->u = dmalloc(3 * N * he);
@@ -691,8 +700,8 @@ void lattice_alloc(Lattice* L) {
   L->force = dmalloc(3 * N * he);
   // Contents start at zero so that reading a field before setting it is defined.
   LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * N * he, L->stream));
-  LB_CUDA(cudaMemsetAsync(L->f[0], 0, 15 * N * fe, L->stream));
-  LB_CUDA(cudaMemsetAsync(L->f[1], 0, 15 * N * fe, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->f[0], 0, fbytes, L->stream));
+  LB_CUDA(cudaMemsetAsync(L->f[1], 0, fbytes, L->stream));
 }
 
 void lattice_free(Lattice* L) {
@@ -776,7 +785,8 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sums(const S* __restrict__ f,
       double m = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
 #pragma unroll
       for (int p = 0; p < 15; ++p) {
-        const double v = dev_from_stored<S>((double)Store<S>::ld(f + p * N + s), p) + w_of(p) * rho0;
+        const double v =
+            dev_from_stored<S>((double)Store<S>::ld(f + fidx<S>(p, s, N)), p) + w_of(p) * rho0;
         m += v;
         jx += cx_of(p) * v;
         jy += cy_of(p) * v;
@@ -868,8 +878,9 @@ static void launch_fused_i(Lattice* L, const FusedArgs& a) {
   LB_CHECK_LAUNCH(1);
 }
 
-// 32-bit site indices while every offset p N + s of the 15 populations fits.
-inline bool fits_int_index(long long n) { return 15 * n < (1ll << 31); }
+// 32-bit site indices while every offset of the 15 populations fits (the
+// reduced-precision buffers hold 15 f_sites(n) values).
+inline bool fits_int_index(long long n) { return 15 * ((n + 31) & ~31ll) < (1ll << 31); }
 
 template <class S, int TZ, int TY, bool SPREAD>
 static void launch_fused(Lattice* L, const FusedArgs& a) {

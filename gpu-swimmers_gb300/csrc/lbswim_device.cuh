@@ -189,6 +189,19 @@ struct Store<__half> {
   __device__ static void st(__half* p, float v) { *p = __float2half_rn(v); }
 };
 
+// Element of population p at site s in a distribution buffer of N sites.
+// FP64 buffers keep the reference's [15][N]; reduced-precision buffers hold
+// blocks of 32 consecutive sites, [ceil(N/32)][15][32], so that the 15 values
+// of a warp's 32 sites lie at fixed offsets p * 32 from one address (the
+// offsets go into the load and store instructions).
+template <class S, class I>
+__host__ __device__ __forceinline__ I fidx(int p, I s, I N) {
+  if constexpr (sizeof(S) == 8)
+    return (I)p * N + s;
+  else
+    return ((s >> 5) * 15 + p) * 32 + (s & 31);
+}
+
 template <class S, class T>
 __device__ __forceinline__ T dev_from_stored(T g, int p) {
   return Store<S>::scaled ? g * T(w_of(p)) : g;

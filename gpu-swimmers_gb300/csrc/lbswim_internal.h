@@ -37,6 +37,12 @@ struct LbswimError {
     ::lbswim::count_launches(nkernels);           \
   } while (0)
 
+// Sites a distribution buffer holds: N, or N rounded up to a multiple of 32 for
+// the blocked layout of reduced-precision buffers (fidx).
+inline long long f_sites(long long N, int precision) {
+  return precision == LBSWIM_F64 ? N : (N + 31) & ~31ll;
+}
+
 inline int elem_bytes(int precision) {
   return precision == LBSWIM_F64 ? 8 : precision == LBSWIM_F32 ? 4 : 2;
 }

@@ -15,6 +15,7 @@
  * Layout: every field is element-slowest SoA, as in the reference
  * (README.md:39).  The site index is i*ny*nz + j*nz + k (lb.cu:55-57).
  *   rho   [N]        u, force  [3][N]        fOld, fNew  [15][N]
+ * (host buffers; lbswim_lattice_device_ptr gives the device layouts)
  *   swimmer r, v, n  [3][n]                  tracer r, s, v  [3][n]
  * Host buffers passed to the *_h2d / *_d2h calls are FP64 whatever the
  * lattice's device precision.
@@ -167,8 +168,10 @@ int lbswim_lattice_synchronize(lbswim_lattice* lat);
 int lbswim_lattice_join(lbswim_lattice* lat);
 /* Device address and element size of a field's current buffer: 8 (FP64
  * lattices); for FP32/BF16/FP16 lattices fOld/fNew are 4 or 2 bytes (f - w_p
- * rho0, divided by w_p for the 16-bit formats), force 4, and rho and u share
- * one buffer of float4 {ux, uy, uz, rho - rho0} per site (16).  rho0 (no
+ * rho0, divided by w_p for the 16-bit formats) in blocks of 32 sites, value p
+ * of site s at ((s / 32) * 15 + p) * 32 + s % 32 (N rounded up to a multiple
+ * of 32), force 4, and rho and u share one buffer of float4
+ * {ux, uy, uz, rho - rho0} per site (16).  rho0 (no
  * reference counterpart) is 1 until InitFromHydro sets it to the mean
  * density, as a float; FP64 lattices have rho0 = 0. */
 int lbswim_lattice_get_rho0(const lbswim_lattice* lat, double* rho0);
