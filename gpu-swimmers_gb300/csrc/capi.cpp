@@ -335,6 +335,7 @@ int lbswim_swimmers_destroy(lbswim_swimmers* sw) {
   cudaFree(W->v);
   cudaFree(W->nv);
   if (W->done) cudaEventDestroy(W->done);
+  if (W->copy) cudaStreamDestroy(W->copy);
   delete W;
   API_END
 }
@@ -399,6 +400,21 @@ int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host) {
   Swimmers* W = SW(sw);
   swimmers_wait(W);
   LB_CUDA(cudaMemcpy(host, sw_field(W, field), sizeof(double) * 3 * W->n, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int lbswim_swimmers_d2h_all(lbswim_swimmers* sw, double* r, double* v, double* n) {
+  API_BEGIN
+  REQUIRE(sw, "swimmers handle is NULL");
+  Swimmers* W = SW(sw);
+  swimmers_wait(W);
+  if (!W->copy) LB_CUDA(cudaStreamCreateWithFlags(&W->copy, cudaStreamNonBlocking));
+  const size_t bytes = sizeof(double) * 3 * W->n;
+  double* dst[3] = {r, v, n};
+  const double* src[3] = {W->r, W->v, W->nv};
+  for (int f = 0; f < 3; ++f)
+    if (dst[f] && bytes) LB_CUDA(cudaMemcpyAsync(dst[f], src[f], bytes, cudaMemcpyDeviceToHost, W->copy));
+  LB_CUDA(cudaStreamSynchronize(W->copy));
   API_END
 }
 

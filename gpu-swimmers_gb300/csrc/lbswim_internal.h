@@ -142,6 +142,7 @@ struct Swimmers {
   // recorded on the stream of the last kernel that read or wrote the arrays,
   // so that host copies wait for that work only (not for other streams)
   cudaEvent_t done = nullptr;
+  cudaStream_t copy = nullptr;  // host copies of several fields in one wait
 };
 
 // Tracers live on the device in a work order binned by position (8^3-site

@@ -105,6 +105,7 @@ _PROTOS = {
     "lbswim_swimmers_move": (C.c_int, [_VP, _VP]),
     "lbswim_swimmers_h2d": (C.c_int, [_VP, C.c_int, _D]),
     "lbswim_swimmers_d2h": (C.c_int, [_VP, C.c_int, _D]),
+    "lbswim_swimmers_d2h_all": (C.c_int, [_VP, _D, _D, _D]),
     "lbswim_swimmers_get_rng": (C.c_int, [_VP, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "lbswim_swimmers_set_rng": (C.c_int, [_VP, C.c_ulonglong, C.c_ulonglong]),
     "lbswim_lattice_interp_velocity": (C.c_int, [_VP, C.c_int, _D, _D]),

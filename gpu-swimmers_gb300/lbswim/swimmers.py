@@ -120,9 +120,9 @@ class Array:
         self.prng.H2D()
 
     def D2H(self):
-        self._r.D2H()
-        self._v.D2H()
-        self._n.D2H()
+        # r, v and n in one call (one wait for the device), then the stream state
+        bufs = [a.view.reshape(-1) for a in (self._r, self._v, self._n)]
+        _lib.check(_lib.lib.lbswim_swimmers_d2h_all(self._h, *[_lib.dptr(b) for b in bufs]))
         self.prng.D2H()
 
     @property

@@ -200,6 +200,9 @@ int lbswim_swimmers_move(lbswim_swimmers* sw, lbswim_lattice* lat);
 /* SharedArray<double>::H2D / D2H of r, v or n (3*n doubles). */
 int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host);
 int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host);
+/* No reference counterpart: the D2H of r, v and n (any may be NULL) with one
+ * wait, for loops that read every field each step. */
+int lbswim_swimmers_d2h_all(lbswim_swimmers* sw, double* r, double* v, double* n);
 /* The random-stream state that SharedArray<RandState> prng holds in the
  * reference (SwimmerArray.h:28): the key seed and the next move step. */
 int lbswim_swimmers_get_rng(const lbswim_swimmers* sw, unsigned long long* seed,
