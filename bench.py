@@ -257,7 +257,7 @@ def reference_arm(args, world, rank):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(args, world),
+            "config": config_dict(args, world, ours=False),
             "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0,
@@ -265,17 +265,19 @@ def reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def config_dict(args, world):
+def config_dict(args, world, ours=True):
     nsw, ntr = scaled_counts(args.size)
-    return {"workload": "coupled step, %d^3 D3Q15 MRT lattice, %d swimmers, %d tracers, %s "
+    cfg = {"workload": "coupled step, %d^3 D3Q15 MRT lattice, %d swimmers, %d tracers, %s "
                         "distributions" % (args.size, nsw, ntr, args.precision),
             "lattice": [args.size] * 3, "swimmers": nsw, "tracers": ntr, "tau": 0.8,
             "precision": args.precision, "parallelism": "replicas x%d" % world,
-            "streams": "lattice on a highest-priority stream (lbswim_lattice_set_stream), "
-                       "tracer moves on their own least-priority stream",
             "l2": "no flush: each step streams %.2f GB of distributions, larger than the "
                   "129 MB L2" % (2 * 15 * args.size ** 3 * {"f64": 8, "f32": 4}.get(
                       args.precision, 2) / 1e9)}
+    if ours:
+        cfg["streams"] = ("lattice on a highest-priority stream (lbswim_lattice_set_stream), "
+                          "tracer moves on their own least-priority stream")
+    return cfg
 
 
 def load_traffic(precision, side):
