@@ -183,3 +183,47 @@ def test_particle_host_copies_are_pinned_and_round_trip():
         vals[name] = (v, arr.data.copy())
     for v, got in vals.values():
         assert np.array_equal(v, got)
+
+
+def test_swimmer_read_back_of_chosen_fields():
+    # lbswim_swimmers_d2h_all copies the fields whose buffers are given and
+    # leaves the others alone
+    from lbswim import _lib, swimmers
+    sw = swimmers.Array(29, swimmers.CommonParams())
+    rng = np.random.default_rng(9)
+    vals = [rng.random((3, 29)) for _ in range(3)]
+    for arr, v in zip((sw.r, sw.v, sw.n), vals):
+        arr[:] = v
+        arr.H2D()
+    r = np.zeros(3 * 29)
+    n = np.zeros(3 * 29)
+    _lib.check(_lib.lib.lbswim_swimmers_d2h_all(sw._h, _lib.dptr(r), None, _lib.dptr(n)))
+    assert np.array_equal(r, vals[0].reshape(-1)) and np.array_equal(n, vals[2].reshape(-1))
+
+
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+def test_blocked_distributions_on_ragged_sizes(precision):
+    # reduced-precision distributions are stored in blocks of 32 sites; with
+    # N = 7*9*11 (not a multiple of 32) fOld goes through H2D/D2H unchanged
+    # (to the format's precision) and a step conserves mass
+    from lbswim import lb
+    lat = lb.Lattice(7, 9, 11, 0.8, 0.8, precision=precision)
+    N = 7 * 9 * 11
+    rng = np.random.default_rng(3)
+    lat.rho[:] = (1.0 + 1e-3 * rng.random(N)).reshape(1, 7, 9, 11)
+    lat.rho.H2D()
+    lat.u[:] = 0.01 * rng.standard_normal((3, 7, 9, 11))
+    lat.u.H2D()
+    lat.InitFromHydro()
+    lat.fOld.D2H()
+    f0 = lat.fOld.data.copy()
+    lat.fOld[:] = f0
+    lat.fOld.H2D()
+    lat.fOld[:] = 0.0
+    lat.fOld.D2H()
+    tol = 1e-7 if precision == "f32" else 1e-4
+    assert np.max(np.abs(lat.fOld.data - f0)) <= tol * np.max(np.abs(f0))
+    m0 = lat.conservation()[0]
+    lat.ZeroForce()
+    lat.Step()
+    assert abs(lat.conservation()[0] - m0) <= 1e-6 * m0
