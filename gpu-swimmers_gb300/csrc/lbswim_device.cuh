@@ -516,27 +516,6 @@ __device__ __forceinline__ bool cover_weight(int x, int o, int n, const T phi[4]
   return true;
 }
 
-// cover_weight with the four weights in a float4 (kept in registers); same
-// selection and, for n < 4, the same summation order.
-__device__ __forceinline__ float pick4(const float4& p, int i) {
-  return i == 0 ? p.x : (i == 1 ? p.y : (i == 2 ? p.z : p.w));
-}
-__device__ __forceinline__ bool cover_weight4(int x, int o, int n, const float4& p, float& w) {
-  if (n >= 4) {
-    int d = x - o;
-    if (d < 0) d += n;
-    if (d > 3) return false;
-    w = pick4(p, d);
-    return true;
-  }
-  float s = 0.f;
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-    if ((o + i) % n == x) s += pick4(p, i);
-  w = s;
-  return true;
-}
-
 // One end's contribution to one force component at a site.  FP64 keeps the
 // reference's order ((phi_x phi_y) phi_z) F (SwimmerArray.cu:64-73); FP32
 // evaluates (phi_y phi_z)(phi_x F) so that phi_x F can be formed once per x
