@@ -338,6 +338,7 @@ __device__ __forceinline__ void end_records_block(
   const int e0 = blk * REC_THREADS;
   const int e = e0 + threadIdx.x;
   const int nends = 2 * nsw;
+  unsigned mbits = 0u;  // largest |F| component of this thread's end, as float bits
   if (e < nends) {
     const int i = e >> 1;
     const bool head = e & 1;
@@ -369,10 +370,13 @@ __device__ __forceinline__ void end_records_block(
       rec.F[a] = (T)F[a];
       m = fmaxf(m, fabsf((float)F[a]));
     }
-    // non-negative floats order like their bit patterns
-    atomicMax(&smax, __float_as_uint(m));
+    mbits = __float_as_uint(m);
     if (bucket_count) bucket_end(e_base + e, rec.o, D, G, bucket_count, bucket_list);
   }
+  // non-negative floats order like their bit patterns: a warp's largest, then
+  // one shared-memory atomic per warp
+  mbits = __reduce_max_sync(0xffffffffu, mbits);
+  if ((threadIdx.x & 31) == 0 && mbits) atomicMax(&smax, mbits);
   __syncthreads();
   if (threadIdx.x == 0 && max_abs_f) atomicMax(max_abs_f, smax);
   const int nrec = min(REC_THREADS, nends - e0);
