@@ -32,6 +32,10 @@ sys.path.insert(0, os.path.join(ROOT, "gpu-swimmers_gb300"))
 
 METRIC = "coupled-step GLUPS & % HBM roofline; p50/p99 latency, batched vs plain FP64"
 L2_BYTES = 129 * 1024 * 1024
+# FP64 operations per site of the reference's DoStep (lb.cu:72-218), each add,
+# multiply and divide counted once: the two dense 15x15 mode transforms (900),
+# the relaxation of the stress modes with forcing (200), the two rates (4)
+REF_DOSTEP_FLOP = 1104
 
 
 def workload(size, nsw, ntr, seed=42, tau=0.8, P=1e-3, l=0.5, alpha=0.01):
@@ -281,7 +285,8 @@ def config_dict(args, world, ours=True):
 
 
 def load_traffic(precision, side):
-    path = os.path.join(ROOT, "profiles", "fused_step_%s_traffic.json" % precision)
+    name = "step_push_f64" if precision == "f64" else "fused_step_%s" % precision
+    path = os.path.join(ROOT, "profiles", "%s_traffic.json" % name)
     try:
         with open(path) as fh:
             rec = json.load(fh)
@@ -365,6 +370,10 @@ def our_arm(args, world, rank, local):
     s_f = {"f64": 8, "f32": 4}.get(args.precision, 2)
     s_h = 8 if args.precision == "f64" else 4
     lb_bytes, step_bytes = algorithmic_bytes(N, nsw, ntr, s_f, s_h)
+    if args.precision == "f64":
+        # k_step_push_f64 reads f and the force and writes f; rho and u come
+        # from the separate CalcHydro kernel
+        lb_bytes = N * (30 * s_f + 3 * s_h)
     peak, peak_kind = measured_peak()
     lb_avg_s = lb_ms / max(lb_n, 1) / 1e3
     achieved = lb_bytes / lb_avg_s / 1e9
@@ -384,6 +393,13 @@ def our_arm(args, world, rank, local):
             "gpu_launches": int(launches), "roofline": roofline,
             "step_roofline": {"achieved": step_ach, "peak": peak, "unit": "GB/s",
                               "frac": step_ach / peak, "bytes_per_step": step_bytes}}
+    if args.precision == "f64":
+        # the FP64 ALU check, in the reference's operations per site;
+        # k_step_push_f64 does the same step with the butterfly transform and
+        # fused multiply-adds, so fewer FP64 instructions
+        line["fp64"] = {"ref_equiv_flop_per_site": REF_DOSTEP_FLOP,
+                        "ref_equiv_tflops": REF_DOSTEP_FLOP * N / lb_avg_s / 1e12,
+                        "kernel": "k_step_push_f64"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_port(min(96, side), 12.0)
     # the batched ensemble and the served stream, each against plain FP64

@@ -160,6 +160,35 @@ def test_system_step_matches_single_calls_bitwise(precision):
         assert np.array_equal(a[k], b[k]), k
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_empty_particle_arrays_leave_the_lattice_alone(precision):
+    # a System holding a swimmer array and a tracer array of zero particles
+    # (the reference allows SwimmerArray(0, ...) and TracerArray(0)) steps the
+    # lattice exactly as ZeroForce, Step and CalcHydro alone do
+    from lbswim import swimmers, tracers
+    from lbswim.System import System
+    case = O.random_case((12, 10, 14), 0, 0, seed=31, u_amp=0.01)
+    lat1 = build_gpu(case, precision)[0]
+    lat2 = build_gpu(case, precision)[0]
+    sw0 = swimmers.Array(0, swimmers.CommonParams())
+    tr0 = tracers.Array(0)
+    system = System(lat1)
+    system.AddThing(sw0)
+    system.AddThing(tr0)
+    system.Step(4)
+    system.Step()
+    for _ in range(5):
+        lat2.ZeroForce()
+        lat2.Step()
+        lat2.CalcHydro()
+    a, b = snapshot(lat1, sw0, tr0), snapshot(lat2, None, None)
+    for k in b:
+        assert np.array_equal(a[k], b[k]), k
+    for k in ("sw_r", "sw_v", "sw_n", "tr_r", "tr_v", "tr_s"):
+        assert a[k].shape == (3, 0), k
+    assert lat1.time_step == lat2.time_step == 5
+
+
 def test_particle_host_copies_are_pinned_and_round_trip():
     # swimmer and tracer host copies live in page-locked memory from
     # lbswim_host_alloc; they keep the FP64 values exactly through H2D/D2H
