@@ -480,7 +480,8 @@ def serving_arm(args):
     """Poisson arrivals of solves (the ensemble distribution plus 96^3 and
     128^3, steps log-uniform in [100, 5000]) served by continuous batching
     under an HBM budget, and the same trace served one solve at a time in
-    plain FP64, each for the same wall time."""
+    plain FP64, each for the same wall time (or the plain one for
+    --serve-plain-seconds)."""
     import torch
     from lbswim import serve
     rng = np.random.default_rng(11)
@@ -490,8 +491,10 @@ def serving_arm(args):
     srv = serve.Server(budget, chunk=64)
     batched = serve.summary(srv.run(trace, args.serve_seconds))
     del srv
-    plain = serve.summary(serve.serve_one_at_a_time(trace, args.serve_seconds, "f64"))
+    plain_s = args.serve_plain_seconds or args.serve_seconds
+    plain = serve.summary(serve.serve_one_at_a_time(trace, plain_s, "f64"))
     return {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
+            "plain_seconds": plain_s,
             "arrivals": len(trace), "hbm_budget_gb": budget / 1e9, "batched_f32": batched,
             "plain_f64": plain,
             "glups_ratio": (batched["glups"] / plain["glups"]) if plain["glups"] else None}
@@ -514,6 +517,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="wall time of each served stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-plain-seconds", type=float, default=0.0,
+                    help="wall time of the plain FP64 stream (0: as --serve-seconds)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
