@@ -63,3 +63,23 @@ def test_python_surface_mirrors_reference_modules():
     import pickle
     cp2 = pickle.loads(pickle.dumps(cp))
     assert cp2.P == 1e-3 and cp2.seed == 1234
+
+
+def test_c_program_builds_against_header_and_library(tmp_path):
+    # tests/c_driver.c uses nothing but include/lbswim_c.h: it compiles as C99
+    # and links against the library (its run is a GPU test)
+    import shutil
+    import subprocess
+    from lbswim import _lib
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    libdir = os.path.dirname(os.path.abspath(_lib.lib._name))
+    exe = str(tmp_path / "c_driver")
+    r = subprocess.run([gcc, "-std=c99", "-O2", "-Wall", "-Werror",
+                        os.path.join(ROOT, "tests", "c_driver.c"),
+                        "-I", os.path.join(ROOT, "include"), "-o", exe, "-L", libdir,
+                        "-l:" + os.path.basename(_lib.lib._name), "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(exe)
