@@ -685,15 +685,18 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
                                double* __restrict__ v, Dims D, const U* __restrict__ u) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ntr) return;
-  double rr[3];
-  for (int d = 0; d < 3; ++d) rr[d] = r[ntr * d + i];
+  double rr[3], ss[3];
+  for (int d = 0; d < 3; ++d) {
+    rr[d] = r[ntr * d + i];
+    ss[d] = s[ntr * d + i];
+  }
   T vv[3];
   interp_velocity<T>(u, D, rr, vv);
   for (int d = 0; d < 3; ++d) {
     const double vd = (double)vv[d];
     v[ntr * d + i] = vd;
     r[ntr * d + i] = wrap_position<T>(rr[d] + vd, D.n[d]);
-    s[ntr * d + i] += vd;
+    s[ntr * d + i] = ss[d] + vd;
   }
 }
 
@@ -1002,9 +1005,13 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
   __shared__ float3 vel[TRACER_MOVE_BLOCK];
   const int i = blk * TRACER_MOVE_BLOCK + threadIdx.x;
   const bool valid = i < ntr;
-  double rr[3] = {0.0, 0.0, 0.0};
+  // s is read with r, so the update at the end waits on no load of its own
+  double rr[3] = {0.0, 0.0, 0.0}, ss[3] = {0.0, 0.0, 0.0};
   if (valid) {
-    for (int d = 0; d < 3; ++d) rr[d] = r[(long long)ntr * d + i];
+    for (int d = 0; d < 3; ++d) {
+      rr[d] = r[(long long)ntr * d + i];
+      ss[d] = s[(long long)ntr * d + i];
+    }
     point_stencil(D, rr, st, threadIdx.x);
   } else {
     st.active[threadIdx.x] = 0;
@@ -1019,7 +1026,7 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
     const double vd = f2d_exact(vv[d]);
     v[(long long)ntr * d + i] = vd;
     r[(long long)ntr * d + i] = advance_position(rr[d], vv[d], D.n[d]);
-    s[(long long)ntr * d + i] += vd;
+    s[(long long)ntr * d + i] = ss[d] + vd;
   }
 }
 
