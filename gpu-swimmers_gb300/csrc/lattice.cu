@@ -884,7 +884,7 @@ inline bool fits_int_index(long long n) { return 15 * ((n + 31) & ~31ll) < (1ll 
 
 template <class S, int TZ, int TY, bool SPREAD>
 static void launch_fused(Lattice* L, const FusedArgs& a) {
-  if (fits_int_index(a.n))
+  if (fits_int_index(a.n) && !(L->compat & LBSWIM_COMPAT_WIDE_INDEX))
     launch_fused_i<S, TZ, TY, SPREAD, int>(L, a);
   else
     launch_fused_i<S, TZ, TY, SPREAD, long long>(L, a);

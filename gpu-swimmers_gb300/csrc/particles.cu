@@ -940,27 +940,29 @@ __device__ __forceinline__ void reduce_lanes(float& vx, float& vy, float& vz) {
 }
 
 // Lane `sub` of the L lanes (4, 8 or 16) of a point gathers z node sub & 3 of
-// y nodes sub >> 2, sub >> 2 + L / 4, ... for the four x nodes.
-template <int L, int NP>
+// y nodes sub >> 2, sub >> 2 + L / 4, ... for the four x nodes.  I is the type
+// of the site offsets: int while N < 2^31.
+template <int L, int NP, class I = int>
 __device__ __forceinline__ void gather_point(const float4* __restrict__ h, const Dims& D,
                                              const StencilSet<NP>& s, int p, int sub,
                                              float& vx, float& vy, float& vz) {
   vx = vy = vz = 0.f;
   if (!s.active[p]) return;
-  const int nz = D.n[2], nynz = D.n[1] * D.n[2];
+  const int nz = D.n[2];
+  const I nynz = (I)D.n[1] * D.n[2];
   const int kz = sub & 3;
   const int z = node_after(s.o[2][p], kz, nz);
   const float wz = s.w[2][kz][p];
-  int xo[4];
+  I xo[4];
   float wx[4];
 #pragma unroll
   for (int ix = 0; ix < 4; ++ix) {
-    xo[ix] = node_after(s.o[0][p], ix, D.n[0]) * nynz;
+    xo[ix] = (I)node_after(s.o[0][p], ix, D.n[0]) * nynz;
     wx[ix] = s.w[0][ix][p];
   }
 #pragma unroll
   for (int jy = sub >> 2; jy < 4; jy += L / 4) {
-    const int yz = node_after(s.o[1][p], jy, D.n[1]) * nz + z;
+    const I yz = (I)node_after(s.o[1][p], jy, D.n[1]) * nz + z;
     const float wyz = s.w[1][jy][p] * wz;
 #pragma unroll
     for (int ix = 0; ix < 4; ++ix) {
@@ -976,15 +978,15 @@ __device__ __forceinline__ void gather_point(const float4* __restrict__ h, const
 // Phase 2: the block's threads, L per point and two points per group at a
 // time, gather the velocity of the NP stencils.  Every thread runs the same
 // number of iterations (NP * L is a multiple of 2 * blockDim).
-template <int L, int NP>
+template <int L, int NP, class I = int>
 __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const Dims& D,
                                              const StencilSet<NP>& st, float3* vel) {
   const int sub = threadIdx.x & (L - 1);
   const int groups = blockDim.x / L;
   for (int p = threadIdx.x / L; p < NP; p += 2 * groups) {
     float ax, ay, az, bx, by, bz;
-    gather_point<L>(h, D, st, p, sub, ax, ay, az);
-    gather_point<L>(h, D, st, p + groups, sub, bx, by, bz);
+    gather_point<L, NP, I>(h, D, st, p, sub, ax, ay, az);
+    gather_point<L, NP, I>(h, D, st, p + groups, sub, bx, by, bz);
     reduce_lanes<L>(ax, ay, az);
     reduce_lanes<L>(bx, by, bz);
     if (sub == 0) {
@@ -997,6 +999,7 @@ __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const
 constexpr int TRACER_MOVE_BLOCK = 256;
 constexpr int TRACER_LANES = 4;  // lanes per interpolation point
 
+template <class I = int>
 __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __restrict__ r,
                                                    double* __restrict__ s,
                                                    double* __restrict__ v, Dims D,
@@ -1017,7 +1020,7 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
     st.active[threadIdx.x] = 0;
   }
   __syncthreads();
-  gather_block<TRACER_LANES>(h, D, st, vel);
+  gather_block<TRACER_LANES, TRACER_MOVE_BLOCK, I>(h, D, st, vel);
   __syncthreads();
   if (!valid) return;
   const float3 w = vel[threadIdx.x];
@@ -1030,10 +1033,11 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
   }
 }
 
+template <class I>
 __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
     int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
     const float4* __restrict__ h) {
-  tracers_move_block(blockIdx.x, ntr, r, s, v, D, h);
+  tracers_move_block<I>(blockIdx.x, ntr, r, s, v, D, h);
 }
 
 // A block takes SWIMMERS_PER_BLOCK swimmers: two stencils (front and rear
@@ -1042,6 +1046,7 @@ constexpr int SWIMMERS_PER_BLOCK = 64;
 constexpr int SWIMMER_LANES = 4;  // lanes per interpolation point
 constexpr int SWIMMER_MOVE_BLOCK = SWIMMERS_PER_BLOCK * SWIMMER_LANES;
 
+template <class I = int>
 __device__ __forceinline__ void swimmers_move_block(
     int blk, int nsw, double* __restrict__ swr, double* __restrict__ swv,
     double* __restrict__ swn, lbswim_common_params c, unsigned long long seed,
@@ -1076,7 +1081,7 @@ __device__ __forceinline__ void swimmers_move_block(
     st.active[B + t] = 0;
   }
   __syncthreads();
-  gather_block<SWIMMER_LANES>(h, D, st, vel);
+  gather_block<SWIMMER_LANES, 2 * SWIMMERS_PER_BLOCK, I>(h, D, st, vel);
   __syncthreads();
   if (!valid) return;
   const float3 w = vel[t], wm = vel[B + t];
@@ -1109,11 +1114,12 @@ __device__ __forceinline__ void swimmers_move_block(
   }
 }
 
+template <class I>
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
     lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
     const float4* __restrict__ h) {
-  swimmers_move_block(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h);
+  swimmers_move_block<I>(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h);
 }
 
 // ---- batched ensembles: per-step reset, end records, moves --------------------
@@ -1458,6 +1464,12 @@ static void append_ends_t(Swimmers* W, Lattice* L) {
   S.pending += nends;
 }
 
+// 64-bit site offsets in the FP32 move kernels: when 32-bit ones would
+// overflow, or when the lattice asks for them (LBSWIM_COMPAT_WIDE_INDEX).
+static bool wide_particle_index(const Lattice* L) {
+  return L->n >= (1ll << 31) || (L->compat & LBSWIM_COMPAT_WIDE_INDEX);
+}
+
 static void swimmers_mark(Swimmers* W, cudaStream_t stream) {
   if (!W->done) LB_CUDA(cudaEventCreateWithFlags(&W->done, cudaEventDisableTiming));
   LB_CUDA(cudaEventRecord(W->done, stream));
@@ -1488,12 +1500,13 @@ void swimmers_move(Swimmers* W, Lattice* L) {
     if (L->precision == LBSWIM_F64)
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u);
-    else if (L->n >= (1ll << 31))  // node offsets beyond int
-      k_swimmers_move<float4, float><<<grid, 256, 0, L->stream>>>(
+    else if (wide_particle_index(L))
+      k_swimmers_move_f32<long long><<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
+                                       SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     else
-      k_swimmers_move_f32<<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
-                            SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
+      k_swimmers_move_f32<int><<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
+                                 SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
     LB_CHECK_LAUNCH(1);
     swimmers_mark(W, L->stream);
@@ -1658,12 +1671,14 @@ static void tracers_move_on(Tracers* T, Lattice* L, cudaStream_t stream) {
   if (L->precision == LBSWIM_F64)
     k_tracers_move<double, double><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
                                                                  (const double*)L->u);
-  else if (L->n >= (1ll << 31))  // node offsets beyond int
-    k_tracers_move<float4, float><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
-                                                                L->hydro);
+  else if (wide_particle_index(L))
+    k_tracers_move_f32<long long><<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK,
+                                    TRACER_MOVE_BLOCK, 0, stream>>>(T->n, T->r, T->s, T->v, D,
+                                                                    L->hydro);
   else
-    k_tracers_move_f32<<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK, TRACER_MOVE_BLOCK,
-                         0, stream>>>(T->n, T->r, T->s, T->v, D, L->hydro);
+    k_tracers_move_f32<int><<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK,
+                              TRACER_MOVE_BLOCK, 0, stream>>>(T->n, T->r, T->s, T->v, D,
+                                                              L->hydro);
   LB_CHECK_LAUNCH(1);
 }
 

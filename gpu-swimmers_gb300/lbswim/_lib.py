@@ -22,7 +22,7 @@ FIELD_RHO, FIELD_U, FIELD_FORCE, FIELD_FOLD, FIELD_FNEW = range(5)
 FIELD_COMPONENTS = {FIELD_RHO: 1, FIELD_U: 3, FIELD_FORCE: 3, FIELD_FOLD: 15, FIELD_FNEW: 15}
 SW_R, SW_V, SW_N = 0, 1, 2
 TR_R, TR_S, TR_V = 0, 1, 2
-COMPAT_INIT_SXZ, COMPAT_SYNC_STEP, COMPAT_EXACT_F64 = 1, 2, 4
+COMPAT_INIT_SXZ, COMPAT_SYNC_STEP, COMPAT_EXACT_F64, COMPAT_WIDE_INDEX = 1, 2, 4, 8
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",
           -5: "not supported"}

@@ -78,6 +78,12 @@ extern "C" {
  * default butterfly transform).  The particle kernels of FP64 lattices always
  * follow the reference's operation order. */
 #define LBSWIM_COMPAT_EXACT_F64 4
+/* FP32/BF16/FP16 lattices: the step and the particle moves use 64-bit site
+ * offsets whatever the lattice size; the results are the same bits.  Without
+ * it they switch to 64-bit offsets by themselves when 32-bit ones would
+ * overflow (15 * N >= 2^31 for the step, N >= 2^31 for the moves).  Batched
+ * ensembles always use 32-bit offsets: their members are smaller. */
+#define LBSWIM_COMPAT_WIDE_INDEX 8
 
 typedef struct lbswim_lattice lbswim_lattice;
 typedef struct lbswim_swimmers lbswim_swimmers;

@@ -41,6 +41,27 @@ def test_f32_mass_conservation():
     assert abs(lat.fOld.data.sum() - m0) / m0 < 1e-7
 
 
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+def test_wide_site_offsets_give_the_same_bits(precision):
+    # Lattices of 15 N >= 2^31 sites (N >= 2^31 for the moves) take the
+    # 64-bit-offset instances of the step and move kernels; the compat flag
+    # makes a small lattice take them too, and nothing but the offsets' type
+    # may change: every field ends the same, bit for bit
+    from lbswim import _lib
+    case = O.random_case((24, 20, 36), 300, 700, seed=12, alpha=0.1, u_amp=0.01)
+    narrow = build_gpu(case, precision)
+    wide = build_gpu(case, precision, compat=_lib.COMPAT_INIT_SXZ | _lib.COMPAT_WIDE_INDEX)
+    for lat, sw, tr, system in (narrow, wide):
+        system.Step(70)  # crosses a tracer re-binning
+        lat.ZeroForce()
+        sw.AddForces(lat)
+        lat.force.D2H()
+    a, b = snapshot(*narrow[:3]), snapshot(*wide[:3])
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert np.abs(a["force"]).max() > 0
+
+
 @pytest.mark.parametrize("shape", [(5, 7, 3), (17, 9, 33), (40, 3, 16), (1, 8, 8), (9, 7, 5), (33, 10, 40)])
 def test_f32_ragged_shapes_match_oracle(shape):
     case = O.random_case(shape, 60, 20, seed=sum(shape), u_amp=0.01)
