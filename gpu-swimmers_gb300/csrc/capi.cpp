@@ -13,13 +13,21 @@
 namespace lbswim {
 static thread_local std::string g_err;
 static std::atomic<unsigned long long> g_launches{0};
+// Calls that may change a lattice, a particle array or their streams; the
+// records a system step prepares for its next step hold only while it stays
+// unchanged (reads and system steps leave it alone).
+static std::atomic<unsigned long long> g_calls{0};
 void set_error(const std::string& m) { g_err = m; }
 void count_launches(unsigned long long n) { g_launches += n; }
 }  // namespace lbswim
 
 using namespace lbswim;
 
-#define API_BEGIN try {
+#define API_BEGIN \
+  try {          \
+    g_calls.fetch_add(1, std::memory_order_relaxed);
+// entry points that change nothing a prepared step depends on
+#define API_BEGIN_READ try {
 #define API_END                                 \
   }                                             \
   catch (const LbswimError& e) {                \
@@ -168,7 +176,7 @@ int lbswim_lattice_d2h(lbswim_lattice* lat, int field, double* host) {
 }
 
 int lbswim_lattice_get_params(const lbswim_lattice* lat, lbswim_lbparams* out) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(out, "out is NULL");
   *out = CLAT(lat)->params;
@@ -176,7 +184,7 @@ int lbswim_lattice_get_params(const lbswim_lattice* lat, lbswim_lbparams* out) {
 }
 
 int lbswim_lattice_get_addressing(const lbswim_lattice* lat, lbswim_addressing* out) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(out, "out is NULL");
   const Lattice* L = CLAT(lat);
@@ -189,7 +197,7 @@ int lbswim_lattice_get_addressing(const lbswim_lattice* lat, lbswim_addressing* 
 }
 
 int lbswim_lattice_get_time_step(const lbswim_lattice* lat, int* out) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(out, "out is NULL");
   *out = CLAT(lat)->time_step;
@@ -204,7 +212,7 @@ int lbswim_lattice_set_time_step(lbswim_lattice* lat, int time_step) {
 }
 
 int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(out, "out is NULL");
   *out = CLAT(lat)->precision;
@@ -335,6 +343,7 @@ int lbswim_swimmers_destroy(lbswim_swimmers* sw) {
   cudaFree(W->v);
   cudaFree(W->nv);
   if (W->done) cudaEventDestroy(W->done);
+  if (W->recorded) cudaEventDestroy(W->recorded);
   if (W->copy) cudaStreamDestroy(W->copy);
   delete W;
   API_END
@@ -349,14 +358,14 @@ int lbswim_swimmers_set_common(lbswim_swimmers* sw, const lbswim_common_params* 
 }
 
 int lbswim_swimmers_get_common(const lbswim_swimmers* sw, lbswim_common_params* out) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(sw && out, "NULL argument");
   *out = reinterpret_cast<const Swimmers*>(sw)->common;
   API_END
 }
 
 int lbswim_swimmers_get_num(const lbswim_swimmers* sw, int* out) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(sw && out, "NULL argument");
   *out = reinterpret_cast<const Swimmers*>(sw)->n;
   API_END
@@ -388,14 +397,16 @@ int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host) {
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
   // the arrays are not bound to one stream: wait for the last kernel that used
-  // them (on whichever stream), not for the whole device
+  // them (on whichever stream), not for the whole device, and for the end
+  // records a system step made of them after its move
   swimmers_wait(W);
+  if (W->recorded) LB_CUDA(cudaEventSynchronize(W->recorded));
   LB_CUDA(cudaMemcpy(sw_field(W, field), host, sizeof(double) * 3 * W->n, cudaMemcpyHostToDevice));
   API_END
 }
 
 int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
   swimmers_wait(W);
@@ -404,7 +415,7 @@ int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host) {
 }
 
 int lbswim_swimmers_d2h_all(lbswim_swimmers* sw, double* r, double* v, double* n) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(sw, "swimmers handle is NULL");
   Swimmers* W = SW(sw);
   swimmers_wait(W);
@@ -420,7 +431,7 @@ int lbswim_swimmers_d2h_all(lbswim_swimmers* sw, double* r, double* v, double* n
 
 int lbswim_swimmers_get_rng(const lbswim_swimmers* sw, unsigned long long* seed,
                             unsigned long long* step) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(sw && seed && step, "NULL argument");
   *seed = reinterpret_cast<const Swimmers*>(sw)->seed;
   *step = reinterpret_cast<const Swimmers*>(sw)->step;
@@ -499,7 +510,7 @@ int lbswim_tracers_destroy(lbswim_tracers* tr) {
 }
 
 int lbswim_tracers_get_num(const lbswim_tracers* tr, int* out) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(tr && out, "NULL argument");
   *out = reinterpret_cast<const Tracers*>(tr)->n;
   API_END
@@ -522,7 +533,7 @@ int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host) {
 }
 
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host) {
-  API_BEGIN
+  API_BEGIN_READ
   REQUIRE(tr && host, "NULL argument");
   REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
   tracers_d2h(TR(tr), field, host);
@@ -616,7 +627,7 @@ int lbswim_ensemble_autotune(lbswim_ensemble* ens) {
 }
 
 int lbswim_lattice_get_rho0(const lbswim_lattice* lat, double* rho0) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(rho0, "rho0 is NULL");
   *rho0 = CLAT(lat)->rho0;
@@ -634,7 +645,7 @@ int lbswim_lattice_conservation(lbswim_lattice* lat, double out[4]) {
 }
 
 int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(tile, "tile is NULL");
   *tile = CLAT(lat)->fused_tile;
@@ -654,7 +665,7 @@ int lbswim_lattice_set_tile(lbswim_lattice* lat, int tile) {
 
 int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, int n_swimmers,
                        lbswim_tracers* const* tracers, int n_tracers, int nsteps) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(n_swimmers >= 0 && n_tracers >= 0 && nsteps >= 0, "counts must be non-negative");
   REQUIRE(n_swimmers == 0 || swimmers, "swimmer list is NULL");
@@ -662,9 +673,14 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
   for (int i = 0; i < n_swimmers; ++i) REQUIRE(swimmers[i], "swimmer handle is NULL");
   for (int i = 0; i < n_tracers; ++i) REQUIRE(tracers[i], "tracer handle is NULL");
   Lattice* L = LAT(lat);
+  // With one swimmer array, each move also records the moved swimmers' ends
+  // for the next step; that step's AddForces takes them unless another call
+  // changed something in between.
+  const unsigned long long calls = g_calls.load(std::memory_order_relaxed);
   for (int t = 0; t < nsteps; ++t) {
     lattice_zero_force(L);  // ZeroForce
-    for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
+    if (n_swimmers != 1 || !swimmers_add_forces_prepared(SW(swimmers[0]), L, calls))
+      for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
     lattice_step(L);
     lattice_calc_hydro(L);
     // Tracers move on their own streams while the swimmers move and the next
@@ -676,7 +692,10 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
       LB_CUDA(cudaEventRecord(L->hydro_ready, L->stream));
       for (int i = 0; i < n_tracers; ++i) tracers_move_async(TR(tracers[i]), L);
     }
-    for (int i = 0; i < n_swimmers; ++i) swimmers_move(SW(swimmers[i]), L);
+    if (n_swimmers == 1)
+      swimmers_move_preparing(SW(swimmers[0]), L, calls);
+    else
+      for (int i = 0; i < n_swimmers; ++i) swimmers_move(SW(swimmers[i]), L);
   }
   API_END
 }

@@ -82,6 +82,25 @@ struct SpreadScratch {
   int* bucket_list = nullptr;        // [bucket_slabs][SLAB_BUCKET_CAP]
   int bucket_slabs = 0;
   int bucket_tile = -1;  // slab shape the buckets hold (Lattice::fused_tile), -1: stale
+  // The next step's end records and slab buckets, written by the swimmer move
+  // of lbswim_system_step; its AddForces takes them in place of recording
+  // again while nothing has changed since (same swimmers, moved by nothing
+  // else, no other API call in between, same slab shape).
+  struct Prepared {
+    void* ends = nullptr;
+    size_t ends_bytes = 0;
+    int capacity_ends = 0;
+    unsigned* bucket_count = nullptr;
+    int* bucket_list = nullptr;
+    int bucket_slabs = 0;
+    unsigned* max_abs_force = nullptr;
+    bool valid = false;
+    const void* owner = nullptr;          // the Swimmers moved
+    unsigned long long owner_step = 0;    // its move counter after that move
+    unsigned long long epoch = 0;         // API-call count then
+    int tile = -1;
+    int nends = 0;
+  } prep;
 };
 
 // What the fused step kernel needs to spread the pending ends itself.
@@ -142,6 +161,9 @@ struct Swimmers {
   // recorded on the stream of the last kernel that read or wrote the arrays,
   // so that host copies wait for that work only (not for other streams)
   cudaEvent_t done = nullptr;
+  // recorded after the end records a system step makes of the moved swimmers
+  // for its next step (they read r and n after the move): uploads wait for it
+  cudaEvent_t recorded = nullptr;
   cudaStream_t copy = nullptr;  // host copies of several fields in one wait
 };
 
@@ -284,6 +306,11 @@ void spread_free(SpreadScratch& S);
 // particles.cu
 void swimmers_add_forces(Swimmers* S, Lattice* L);
 void swimmers_move(Swimmers* S, Lattice* L);
+// lbswim_system_step with one swimmer array: AddForces from the records the
+// last move prepared (false: nothing prepared that still holds), and the move
+// that prepares them for the next step.  epoch counts the API calls made.
+bool swimmers_add_forces_prepared(Swimmers* S, Lattice* L, unsigned long long epoch);
+void swimmers_move_preparing(Swimmers* S, Lattice* L, unsigned long long epoch);
 // Wait on the host for the last kernel that used the swimmer arrays.
 void swimmers_wait(Swimmers* S);
 void tracers_move(Tracers* T, Lattice* L);

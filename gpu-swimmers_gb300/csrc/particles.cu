@@ -295,8 +295,6 @@ __device__ __forceinline__ void slab_shape_of_dev(int tile, int T[3]) {
   T[2] = tile == 1 ? 16 : 32;
 }
 
-// One record per dipole end: e = 2i is the tail, 2i + 1 the head.  Records are
-// assembled in shared memory and written out as one contiguous block.
 // List end e under every slab of grid G whose extended region its stencil
 // touches (at most SLAB_BUCKET_CAP ends are kept per slab; the count goes on).
 __device__ __forceinline__ void bucket_end(int e, const int o[3], const Dims& D, const TileGrid& G,
@@ -1255,6 +1253,13 @@ static void free_lists(TileLists& TL) {
 }
 
 void spread_free(SpreadScratch& S) {
+  {
+    SpreadScratch::Prepared& P = S.prep;
+    void* ptrs[] = {P.ends, P.bucket_count, P.bucket_list, P.max_abs_force};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    P = SpreadScratch::Prepared();
+  }
   if (S.ends) cudaFree(S.ends);
   if (S.max_abs_force) cudaFree(S.max_abs_force);
   if (S.bucket_count) cudaFree(S.bucket_count);
@@ -1512,6 +1517,87 @@ void swimmers_move(Swimmers* W, Lattice* L) {
     swimmers_mark(W, L->stream);
   }
   W->step++;
+}
+
+// The move of lbswim_system_step with one swimmer array: on reduced-precision
+// lattices it is followed by the records and slab buckets of the moved
+// swimmers' ends, made into the lattice's prepared set, which the next step's
+// AddForces takes if nothing changed in between (swimmers_add_forces_prepared).
+// A read-back of the swimmers waits for the move only; an upload also waits
+// for these records.
+void swimmers_move_preparing(Swimmers* W, Lattice* L, unsigned long long epoch) {
+  SpreadScratch::Prepared& P = L->spread.prep;
+  P.valid = false;
+  swimmers_move(W, L);
+  if (W->n <= 0 || L->precision == LBSWIM_F64) return;
+  const TileGrid G = slab_grid(L);
+  const int nslabs = G.nt[0] * G.nt[1] * G.nt[2];
+  const int nends = 2 * W->n;
+  const size_t rec = sizeof(EndRecord<float>);
+  if (P.capacity_ends < nends || P.bucket_slabs != nslabs || !P.max_abs_force) {
+    // the buffers may still be read by earlier work on the stream
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    if (P.capacity_ends < nends) {
+      if (P.ends) cudaFree(P.ends);
+      P.ends = nullptr;
+      P.capacity_ends = 0;
+      const int cap = std::max(nends + nends / 2, 64);
+      LB_CUDA(cudaMalloc(&P.ends, rec * cap));
+      P.capacity_ends = cap;
+      P.ends_bytes = rec * cap;
+    }
+    if (P.bucket_slabs != nslabs) {
+      if (P.bucket_count) cudaFree(P.bucket_count);
+      if (P.bucket_list) cudaFree(P.bucket_list);
+      P.bucket_count = nullptr;
+      P.bucket_list = nullptr;
+      P.bucket_slabs = 0;
+      LB_CUDA(cudaMalloc(&P.bucket_count, sizeof(unsigned) * nslabs));
+      LB_CUDA(cudaMalloc(&P.bucket_list, sizeof(int) * (size_t)nslabs * SLAB_BUCKET_CAP));
+      P.bucket_slabs = nslabs;
+    }
+    if (!P.max_abs_force) LB_CUDA(cudaMalloc(&P.max_abs_force, sizeof(unsigned)));
+  }
+  LB_CUDA(cudaMemsetAsync(P.bucket_count, 0, sizeof(unsigned) * nslabs, L->stream));
+  LB_CUDA(cudaMemsetAsync(P.max_abs_force, 0, sizeof(unsigned), L->stream));
+  k_end_records<float><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
+      W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L), (EndRecord<float>*)P.ends, 0,
+      P.max_abs_force, G, P.bucket_count, P.bucket_list);
+  LB_CHECK_LAUNCH(1);
+  if (!W->recorded) LB_CUDA(cudaEventCreateWithFlags(&W->recorded, cudaEventDisableTiming));
+  LB_CUDA(cudaEventRecord(W->recorded, L->stream));
+  P.valid = true;
+  P.owner = W;
+  P.owner_step = W->step;
+  P.epoch = epoch;
+  P.tile = L->fused_tile;
+  P.nends = nends;
+}
+
+// AddForces of W (right after ZeroForce) from the prepared set, when the last
+// thing that happened to W and to this lattice was that preparing move.
+bool swimmers_add_forces_prepared(Swimmers* W, Lattice* L, unsigned long long epoch) {
+  SpreadScratch& S = L->spread;
+  SpreadScratch::Prepared& P = S.prep;
+  if (!P.valid || P.owner != W || P.owner_step != W->step || P.epoch != epoch ||
+      P.tile != L->fused_tile || L->precision == LBSWIM_F64 || S.pending != 0 || S.stepped ||
+      P.nends != 2 * W->n)
+    return false;
+  const TileGrid G = slab_grid(L);
+  if (P.bucket_slabs != G.nt[0] * G.nt[1] * G.nt[2]) return false;
+  std::swap(S.ends, P.ends);
+  std::swap(S.ends_bytes, P.ends_bytes);
+  std::swap(S.capacity_ends, P.capacity_ends);
+  std::swap(S.bucket_count, P.bucket_count);
+  std::swap(S.bucket_list, P.bucket_list);
+  std::swap(S.bucket_slabs, P.bucket_slabs);
+  std::swap(S.max_abs_force, P.max_abs_force);
+  S.bucket_tile = L->fused_tile;
+  S.pending = P.nends;
+  P.valid = false;
+  swimmers_mark(W, L->stream);
+  L->force_version++;
+  return true;
 }
 
 // ---- tracer work order ------------------------------------------------------------

@@ -160,6 +160,46 @@ def test_system_step_matches_single_calls_bitwise(precision):
         assert np.array_equal(a[k], b[k]), k
 
 
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+def test_system_steps_across_calls_match_single_calls(precision):
+    # The swimmer move of a system step also records the next step's dipole
+    # ends; the next System.Step takes them unless another call came in
+    # between.  One Step per call with read-backs (which change nothing), then
+    # the swimmer positions written back (same values) and P changed between
+    # calls: the same bits as the README's single calls throughout.
+    case = O.random_case((24, 16, 32), 80, 300, seed=45, alpha=0.1, u_amp=0.01)
+    lat1, sw1, tr1, system1 = build_gpu(case, precision)
+    lat2, sw2, tr2, _ = build_gpu(case, precision)
+
+    def single(n):
+        for _ in range(n):
+            lat2.ZeroForce()
+            sw2.AddForces(lat2)
+            lat2.Step()
+            lat2.CalcHydro()
+            sw2.Move(lat2)
+            tr2.Move(lat2)
+
+    for _ in range(30):
+        system1.Step()
+        sw1.D2H()
+        assert lat1.time_step > 0
+    single(30)
+    for sw in (sw1, sw2):
+        sw.D2H()
+        sw.H2D()
+    for _ in range(10):
+        system1.Step()
+    single(10)
+    for sw in (sw1, sw2):
+        sw.common.P = 2e-3
+    system1.Step(12)
+    single(12)
+    a, b = snapshot(lat1, sw1, tr1), snapshot(lat2, sw2, tr2)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_empty_particle_arrays_leave_the_lattice_alone(precision):
     # a System holding a swimmer array and a tracer array of zero particles
