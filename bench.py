@@ -173,27 +173,39 @@ def build_objects(case, precision):
     return lat, sw, tr, system
 
 
-def upload(case, lat, sw, tr):
-    """Host -> device copy of the whole initial state; returns bytes moved."""
+def fill_host(case, lat, sw, tr):
+    """Write the initial state into the objects' (page-locked) host copies."""
     nx, ny, nz = case["size"]
     N = nx * ny * nz
     lat.rho[:] = np.broadcast_to(case["rho"], (N,)).reshape(1, nx, ny, nz)
-    lat.rho.H2D()
     lat.u[:] = np.broadcast_to(case["u"], (3 * N,)).reshape(3, nx, ny, nz)
-    lat.u.H2D()
-    lat.ZeroForce()
     s = case["swimmers"]
     sw.r[:] = s["r"]
     sw.n[:] = s["nvec"]
     sw.v[:] = s["v"]
-    sw.H2D()
     t = case["tracers"]
     tr.r[:] = t["r"]
     tr.v[:] = t["v"]
     tr.s[:] = 0.0
+
+
+def push(case, lat, sw, tr):
+    """Host -> device copy of the whole initial state from the host copies, then
+    InitFromHydro; returns the bytes copied."""
+    lat.rho.H2D()
+    lat.u.H2D()
+    lat.ZeroForce()
+    sw.H2D()
     tr.H2D()
     lat.InitFromHydro()
-    return 8 * N * 4 + 8 * 9 * s["n"] + 16 + 8 * 9 * t["n"]
+    N = int(np.prod(case["size"]))
+    return 8 * N * 4 + 8 * 9 * case["swimmers"]["n"] + 16 + 8 * 9 * case["tracers"]["n"]
+
+
+def upload(case, lat, sw, tr):
+    """Host fill and host -> device copy of the whole initial state."""
+    fill_host(case, lat, sw, tr)
+    return push(case, lat, sw, tr)
 
 
 def algorithmic_bytes(N, nsw, ntr, s_f, s_h):
@@ -203,48 +215,57 @@ def algorithmic_bytes(N, nsw, ntr, s_f, s_h):
     return lb_bytes, lb_bytes + 120 * nsw + 120 * ntr
 
 
-def run_cpu_port(side, steps_budget_s, min_steps=3, threads=None, case=None):
-    """Time the FP64 CPU restatement of the reference on a side^3 sample."""
+def oracle_module():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    threads = threads or os.cpu_count()
-    O.set_threads(threads)
-    if case is None:
-        nsw, ntr = scaled_counts(side)
-        case = workload((side, side, side), nsw, ntr)
+    O.set_threads(os.cpu_count())
+    return O
+
+
+def cpu_side(O, size, per_step_budget_s):
+    """Largest lattice side <= size whose coupled FP64 oracle step (particles at
+    the 256^3 workload's densities) fits per_step_budget_s, calibrated on 64^3."""
+    nsw, ntr = scaled_counts(64)
+    cal = O.make_system(workload((64, 64, 64), nsw, ntr))
+    cal.step(1)
+    t0 = time.perf_counter()
+    cal.step(2)
+    per_site = (time.perf_counter() - t0) / 2 / 64 ** 3
+    return int(max(16, min(size, (per_step_budget_s / per_site) ** (1.0 / 3.0))))
+
+
+def run_cpu_port(size, budget_s, min_steps=3):
+    """Time the FP64 CPU restatement of the reference (all host threads) on the
+    size^3 workload, or on the largest cube that fits the budget."""
+    O = oracle_module()
+    side = cpu_side(O, size, budget_s / (min_steps + 1))
+    nsw, ntr = scaled_counts(side)
+    case = workload((side, side, side), nsw, ntr)
     s = O.make_system(case)
     s.step(1)
     t0 = time.perf_counter()
     n = 0
-    while n < min_steps or time.perf_counter() - t0 < steps_budget_s:
+    while n < min_steps or time.perf_counter() - t0 < budget_s:
         s.step(1)
         n += 1
     dt = time.perf_counter() - t0
     N = side ** 3
     return {"value": N * n / dt / 1e9, "unit": "GLUPS", "cores": O.get_threads(), "kind": "port",
-            "sample": "%d^3 lattice, %d swimmers, %d tracers (256^3 densities), %d coupled FP64 "
-                      "steps in %.1f s, oracle/lbswim_oracle.c with OpenMP"
-                      % (side, case["swimmers"]["n"], case["tracers"]["n"], n, dt)}
+            "sample": "%d^3 lattice, %d swimmers, %d tracers%s, %d coupled FP64 steps in %.1f s "
+                      "after one untimed step, oracle/lbswim_oracle.c with OpenMP"
+                      % (side, nsw, ntr, "" if side == size else
+                         " (the %d^3 workload's densities)" % size, n, dt)}
 
 
 def reference_arm(args, world, rank):
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    O.build()
-    threads = os.cpu_count()
-    O.set_threads(threads)
-    # calibrate the per-site cost on a 64^3 sample, then size the sample so the
-    # whole warm-up + timed run stays within about two minutes
-    nsw, ntr = scaled_counts(64)
-    cal = O.make_system(workload((64, 64, 64), nsw, ntr))
-    t0 = time.perf_counter()
-    cal.step(2)
-    per_site = (time.perf_counter() - t0) / 2 / 64 ** 3
-    budget = 120.0 / max(1, args.steps + args.warmup)
-    side = int(max(16, min(args.size, (budget / per_site) ** (1.0 / 3.0))))
+    O = oracle_module()
+    threads = O.get_threads()
+    # size the sample so the whole warm-up + timed run stays within about two
+    # minutes (the full 256^3 workload takes ~0.4 s per step on 16 Grace cores)
+    side = cpu_side(O, args.size, 120.0 / max(1, args.steps + args.warmup))
     nsw, ntr = scaled_counts(side)
     case = workload((side, side, side), nsw, ntr)
     s = O.make_system(case)
@@ -254,14 +275,15 @@ def reference_arm(args, world, rank):
     dt = time.perf_counter() - t0
     N = side ** 3
     value = N * args.steps / dt / 1e9
-    sample = ("%d^3 lattice, %d swimmers, %d tracers (the %d^3 workload's densities), FP64, "
-              "oracle/lbswim_oracle.c (the reference's method restated in C) on %d threads"
-              % (side, nsw, ntr, args.size, threads))
+    sample = ("%d^3 lattice, %d swimmers, %d tracers%s, FP64, oracle/lbswim_oracle.c (the "
+              "reference's method restated in C) on %d threads"
+              % (side, nsw, ntr, "" if side == args.size else
+                 " (the %d^3 workload's densities)" % args.size, threads))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(args, world, ours=False),
+            "config": config_dict(args, world, precision="f64", ours=False),
             "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0,
@@ -269,15 +291,16 @@ def reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def config_dict(args, world, ours=True):
+def config_dict(args, world, precision=None, ours=True):
+    precision = precision or args.precision
     nsw, ntr = scaled_counts(args.size)
     cfg = {"workload": "coupled step, %d^3 D3Q15 MRT lattice, %d swimmers, %d tracers, %s "
-                        "distributions" % (args.size, nsw, ntr, args.precision),
+                        "distributions" % (args.size, nsw, ntr, precision),
             "lattice": [args.size] * 3, "swimmers": nsw, "tracers": ntr, "tau": 0.8,
-            "precision": args.precision, "parallelism": "replicas x%d" % world,
+            "precision": precision, "parallelism": "replicas x%d" % world,
             "l2": "no flush: each step streams %.2f GB of distributions, larger than the "
                   "129 MB L2" % (2 * 15 * args.size ** 3 * {"f64": 8, "f32": 4}.get(
-                      args.precision, 2) / 1e9)}
+                      precision, 2) / 1e9)}
     if ours:
         cfg["streams"] = ("lattice on a highest-priority stream (lbswim_lattice_set_stream), "
                           "tracer moves on their own least-priority stream")
@@ -294,6 +317,61 @@ def load_traffic(precision, side):
         return rec["dram_bytes_per_site"] * side ** 3
     except Exception:
         return None
+
+
+def timed_steps(lat, system, steps, stream):
+    """CUDA-event time (ms) of `steps` coupled steps on the lattice's stream and
+    the LB step kernel's own event time (total ms, launches)."""
+    import torch
+    lat.set_timing(True)
+    lat.read_timing()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        system.Step()
+    lat.join()  # the last tracer moves run on the tracers' stream
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    lb_ms, lb_n = lat.read_timing()
+    lat.set_timing(False)
+    return ev0.elapsed_time(ev1), lb_ms, lb_n
+
+
+def f64_arm(args, case, stream):
+    """The reference's own method and precision (FP64 storage and arithmetic)
+    on the same workload, device-resident, for the like-for-like ratio with the
+    FP64 reference arm."""
+    import torch
+    N = int(np.prod(case["size"]))
+    nsw, ntr = case["swimmers"]["n"], case["tracers"]["n"]
+    lat, sw, tr, system = build_objects(case, "f64")
+    lat.set_stream(stream.cuda_stream)
+    upload(case, lat, sw, tr)
+    for _ in range(3):
+        system.Step()
+    torch.cuda.synchronize()
+    ms, lb_ms, lb_n = timed_steps(lat, system, args.f64_steps, stream)
+    ms_step = ms / args.f64_steps
+    peak, _ = measured_peak()
+    kernel_s = lb_ms / max(lb_n, 1) / 1e3
+    # k_step_push_f64 reads f and the force and writes f (rho, u come from the
+    # separate CalcHydro kernel)
+    kernel_bytes = N * (30 * 8 + 3 * 8)
+    _, step_bytes = algorithmic_bytes(N, nsw, ntr, 8, 8)
+    out = {"precision": "f64", "steps": args.f64_steps, "warmup": 3,
+           "ms_per_step": ms_step, "glups": N / (ms_step / 1e3) / 1e9,
+           "step_roofline": {"achieved": step_bytes / (ms_step / 1e3) / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
+                             "bytes_per_step": step_bytes},
+           "kernel": {"name": "k_step_push_f64", "ms": kernel_s * 1e3,
+                      "bytes_per_launch": kernel_bytes,
+                      "hbm_frac": kernel_bytes / kernel_s / 1e9 / peak,
+                      "ref_equiv_flop_per_site": REF_DOSTEP_FLOP,
+                      "ref_equiv_tflops": REF_DOSTEP_FLOP * N / kernel_s / 1e12,
+                      "bound": "fp64 pipe (the kernel's FP64 instructions, not HBM)"}}
+    del system, sw, tr, lat
+    return out
 
 
 def our_arm(args, world, rank, local):
@@ -347,25 +425,36 @@ def our_arm(args, world, rank, local):
     ms_step = ms / args.steps
     value = N * args.steps * world / (ms / 1e3) / 1e9
 
-    # end to end through the public API: upload, init, K steps each followed by
-    # the swimmer read-back of the README loop, final read-back of rho and u
+    # End to end through the public API, from the page-locked host copies the
+    # initial state was written into beforehand: upload of rho, u and the
+    # particles, InitFromHydro, K steps each followed by the swimmer read-back
+    # of the README loop, and the final read-back of rho and u.
+    fill_host(case, lat, sw, tr)
     barrier()
     t0 = time.perf_counter()
-    h2d = upload(case, lat, sw, tr)
+    h2d = push(case, lat, sw, tr)
+    lat.synchronize()
+    t1 = time.perf_counter()
     d2h = 0
     for _ in range(args.steps):
         system.Step()
         sw.D2H()
         d2h += 8 * 9 * nsw + 16
+    lat.synchronize()
+    t2 = time.perf_counter()
     lat.rho.D2H()
     lat.u.D2H()
     d2h += 8 * 4 * N
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, world)
+    t3 = time.perf_counter()
+    e2e_s = max_over_ranks(t3 - t0, world)
     e2e = {"value": N * args.steps * world / e2e_s / 1e9, "unit": "GLUPS",
            "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
-           "api": "lbswim.System.Step() + swimmers.Array.D2H() per step (Python -> C ABI)"}
+           "api": "lbswim.System.Step() + swimmers.Array.D2H() per step (Python -> C ABI)",
+           "steps": args.steps,
+           "pieces_ms": {"upload_and_init": (t1 - t0) * 1e3, "steps_with_readback": (t2 - t1) * 1e3,
+                         "final_readback": (t3 - t2) * 1e3},
+           "host_fill": "outside the timed region (written into page-locked host copies first)"}
 
     s_f = {"f64": 8, "f32": 4}.get(args.precision, 2)
     s_h = 8 if args.precision == "f64" else 4
@@ -400,8 +489,12 @@ def our_arm(args, world, rank, local):
         line["fp64"] = {"ref_equiv_flop_per_site": REF_DOSTEP_FLOP,
                         "ref_equiv_tflops": REF_DOSTEP_FLOP * N / lb_avg_s / 1e12,
                         "kernel": "k_step_push_f64"}
+    del system, sw, tr, lat
+    if args.precision != "f64" and args.f64_steps > 0:
+        # the same workload in the reference's precision, beside the headline
+        line["f64"] = f64_arm(args, case, stream)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = run_cpu_port(min(96, side), 12.0)
+        line["cpu_baseline"] = run_cpu_port(side, args.cpu_seconds)
     # the batched ensemble and the served stream, each against plain FP64
     # one solve at a time (every rank runs its own replica)
     if args.ens_members > 0:
@@ -509,6 +602,10 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f64", "f32", "bf16", "f16"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="timed CPU work of the cpu_baseline leg")
+    ap.add_argument("--f64-steps", type=int, default=20,
+                    help="steps of the FP64 run of the same workload (0: skip)")
     ap.add_argument("--ens-members", type=int, default=512,
                     help="batched-ensemble members (0: skip the ensemble figures)")
     ap.add_argument("--ens-steps", type=int, default=1000)

@@ -180,32 +180,38 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
   }
 }
 
-// Equilibrium from rho, u, lb.cu:314-371 (compat_sxz reproduces lb.cu:356).
-// rho, u come from the FP64 SoA fields or, when packed is set, the float4 ones,
-// whose w holds rho - rho_w; it is rewritten as rho - rho0 for the new rho0.
-template <class S>
+// Equilibrium from rho, u, lb.cu:314-371 (compat_sxz reproduces lb.cu:356),
+// FP64 lattices: rho, u from the FP64 SoA fields.
 __global__ void k_init_from_hydro(const double* __restrict__ rho, const double* __restrict__ u,
-                                  float4* __restrict__ packed, S* __restrict__ f, long long N,
-                                  double rho_w, double rho0, int compat_sxz) {
+                                  double* __restrict__ f, long long N, int compat_sxz) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
-    double r, ux, uy, uz;
-    if (packed) {
-      const float4 h = packed[s];
-      r = (double)h.w + rho_w;
-      packed[s].w = (float)(r - rho0);
-      ux = h.x;
-      uy = h.y;
-      uz = h.z;
-    } else {
-      r = rho[s];
-      ux = u[s];
-      uy = u[N + s];
-      uz = u[2 * N + s];
-    }
+    const double r = rho[s], ux = u[s], uy = u[N + s], uz = u[2 * N + s];
     double out[15];
-    project<double>(r - rho0, r * ux, r * uy, r * uz, r * ux * ux, r * uy * uy, r * uz * uz,
+    project<double>(r, r * ux, r * uy, r * uz, r * ux * ux, r * uy * uy, r * uz * uz,
                     r * ux * uy, compat_sxz ? r * ux * uy : r * ux * uz, r * uy * uz, out);
+#pragma unroll
+    for (int p = 0; p < 15; ++p) f[fidx<double>(p, s, N)] = out[p];
+  }
+}
+
+// The same for FP32/BF16/FP16 lattices, in FP32 (the stored deviations carry
+// FP32 precision or less, so FP64 arithmetic would buy nothing): rho, u from
+// the packed float4 fields, whose w holds rho - rho_w; it is rewritten as
+// R = rho - rho0 for the new reference density, R = w + (rho_w - rho0).
+template <class S>
+__global__ void k_init_from_hydro_packed(float4* __restrict__ packed, S* __restrict__ f,
+                                         long long N, float drho, float rho0, int compat_sxz) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
+       s += (long long)gridDim.x * blockDim.x) {
+    const float4 h = packed[s];
+    const float R = h.w + drho;
+    packed[s].w = R;
+    const float r = rho0 + R, ux = h.x, uy = h.y, uz = h.z;
+    const float jx = r * ux, jy = r * uy, jz = r * uz;
+    float out[15];
+    project<float>(R, jx, jy, jz, jx * ux, jy * uy, jz * uz, jx * uy,
+                   compat_sxz ? jx * uy : jx * uz, jy * uz, out);
 #pragma unroll
     for (int p = 0; p < 15; ++p) Store<S>::st(f + fidx<S>(p, s, N), stored_from_dev<S>(out[p], p));
   }
@@ -756,13 +762,12 @@ template <class S>
 static void init_from_hydro_t(Lattice* L, double rho_w) {
   const long long N = L->n;
   const int compat = (L->compat & LBSWIM_COMPAT_INIT_SXZ) ? 1 : 0;
-  if (L->precision == LBSWIM_F64)
-    k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        (const double*)L->rho, (const double*)L->u, nullptr, (S*)L->f[L->cur], N, 0.0, 0.0,
-        compat);
+  if constexpr (sizeof(S) == 8)
+    k_init_from_hydro<<<grid_for(N, 256), 256, 0, L->stream>>>(
+        (const double*)L->rho, (const double*)L->u, (double*)L->f[L->cur], N, compat);
   else
-    k_init_from_hydro<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
-        nullptr, nullptr, L->hydro, (S*)L->f[L->cur], N, rho_w, L->rho0, compat);
+    k_init_from_hydro_packed<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
+        L->hydro, (S*)L->f[L->cur], N, (float)(rho_w - L->rho0), (float)L->rho0, compat);
   LB_CHECK_LAUNCH(1);
 }
 

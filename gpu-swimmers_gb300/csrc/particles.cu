@@ -1875,14 +1875,20 @@ void spread_forces_noalloc(const double* r, const double* nv, int nsw, double P,
   }
   D.N = (long long)size[0] * size[1] * size[2];
   const long long nbins = (long long)D.nb[0] * D.nb[1] * D.nb[2];
-  const int nends = 2 * nsw;
-  if (nends > NOALLOC_MAX_ENDS)
-    throw LbswimError{LBSWIM_EINVAL, "more swimmers than the allocation-free limit of " +
+  // Every limit is checked before anything is enqueued (the swimmer count
+  // before it is doubled, so that no count can wrap past the check).
+  if (nsw < 0 || nsw > LBSWIM_NOALLOC_MAX_SWIMMERS)
+    throw LbswimError{LBSWIM_EINVAL, "swimmer count outside the allocation-free limit of 0.." +
                                          std::to_string(LBSWIM_NOALLOC_MAX_SWIMMERS)};
   if (nbins > NOALLOC_MAX_BINS)
     throw LbswimError{LBSWIM_EINVAL,
                       "lattice larger than the allocation-free limit (" +
                           std::to_string(NOALLOC_MAX_BINS) + " spread bins of 4^3 sites)"};
+  // the gather's grid is (ceil(nz / 32), ceil(ny / 8), nx) blocks
+  if (D.n[0] > 65535 || (D.n[1] + 7) / 8 > 65535)
+    throw LbswimError{LBSWIM_EINVAL, "lattice axes beyond the allocation-free limit "
+                                     "(nx <= 65535, ny <= 524280)"};
+  const int nends = 2 * nsw;
   unsigned char* base = noalloc_scratch_for_current_device();
   unsigned* bin_count = (unsigned*)(base + NA_COUNT);
   unsigned* bin_start = (unsigned*)(base + NA_START);

@@ -236,21 +236,24 @@ int lbswim_rng_draws(unsigned long long seed, int n, unsigned long long step, fl
 /* No counterpart in the reference: it always allocates through SharedArray.
  * Spreads the dipole forces of nsw swimmers (the computation of
  * lbswim_swimmers_add_forces) into a caller-owned FP64 force field without
- * allocating any memory, for callers that cannot call cudaMalloc: code running
- * inside CUDA stream capture, real-time loops where an allocation's implicit
- * synchronisation or failure is not acceptable, and hosts that own all device
- * memory through their own allocator.
+ * allocating any memory.  It is meant for callers that cannot call
+ * cudaMalloc: a host application that owns all device memory through its own
+ * pool allocator and lets plug-in code use only the buffers it hands out, and
+ * real-time loops in which an allocation's implicit device synchronisation,
+ * or its failure half way through a time step, is not acceptable.
  * All pointers are device pointers owned by the caller: r and n are the
  * swimmers' positions and orientations, [3][nsw] doubles; force is
  * [3][nx*ny*nz] doubles, overwritten (accumulate = 0) or added to
  * (accumulate != 0).  Work is enqueued on `stream` (a cudaStream_t, NULL for
- * the legacy default stream).  Scratch lives in one static device array:
- * nsw may be at most LBSWIM_NOALLOC_MAX_SWIMMERS and the lattice at most
- * LBSWIM_NOALLOC_MAX_SPREAD_BINS spread bins (ceil(nx/4)*ceil(ny/4)*ceil(nz/4));
- * larger inputs are rejected with LBSWIM_EINVAL before any work is enqueued.
+ * the legacy default stream).  Scratch lives in one static device array of
+ * about 6.5 MB: nsw may be at most LBSWIM_NOALLOC_MAX_SWIMMERS, the lattice at
+ * most LBSWIM_NOALLOC_MAX_SPREAD_BINS spread bins
+ * (ceil(nx/4)*ceil(ny/4)*ceil(nz/4)), nx at most 65535 and ny at most 524280;
+ * other inputs are rejected with LBSWIM_EINVAL before any work is enqueued.
  * The first call on a device looks up the array's device address (with that
- * device current), so make that first call before any stream capture begins.
- * All calls on a device share the one scratch array: calls whose work
+ * device current); make that first call before any stream capture begins.
+ * All calls on a device share the one scratch array, which keeps the last
+ * call's contents (the call clears what must start at zero): calls whose work
  * overlaps on the GPU (different streams, or concurrent host threads) race and
  * give wrong results; serialise them on one stream. */
 int lbswim_spread_forces_noalloc(const double* r, const double* n, int nsw, double P, double l,

@@ -10,7 +10,7 @@ oracle/_ref/libref.so.  The cuRAND header is replaced by
 oracle/ref_shim/curand_kernel.h (the project's counter-based stream), and the
 shim header makes __global__/__device__ empty.
 
-Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+Usage: python oracle/build_ref.py [REFERENCE_ROOT]   (default: $LBSWIM_REFERENCE_ROOT)
 """
 import os
 import re
@@ -18,13 +18,21 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+# Where the reference checkout lies: $LBSWIM_REFERENCE_ROOT, else the path of
+# this build machine's read-only copy.
+DEFAULT_REF = os.environ.get("LBSWIM_REFERENCE_ROOT", "/root/reference")
 SOURCES = ["Shared.cu", "lb.cu", "SwimmerArray.cu", "TracerArray.cu"]
 LAUNCH = re.compile(r"(\w+)\s*<<<(.*?)>>>\s*\((.*?)\)\s*;", re.S)
 
 
 def translate(text):
     return LAUNCH.sub(lambda m: "ref_launch(%s, [&]{ %s(%s); });" % (m.group(2), m.group(1), m.group(3)), text)
+
+
+def reference_root():
+    """The reference checkout if its kernel sources are present, else None
+    (machines without the reference skip everything that needs it)."""
+    return DEFAULT_REF if os.path.isdir(os.path.join(DEFAULT_REF, "lbswim", "liblbswim")) else None
 
 
 def build(ref_root=DEFAULT_REF, out_dir=None, quiet=False):

@@ -10,16 +10,19 @@ parameters of the reference are common to an array), l = 0.5, orientations
 uniform on the sphere; 1,048,576 tracers; 1000 steps.  Smaller sizes scale the
 particle counts with the volume.
 
-    python -m lbswim.precision_study [--size 384] [--steps 1000] [--out result.json]
+    python precision_study.py [--size 384] [--steps 1000] [--out result.json]
 """
 import argparse
 import json
+import os
+import sys
 import time
 
 import numpy as np
 
-from . import lb, swimmers, tracers
-from .System import System
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "gpu-swimmers_gb300"))
+from lbswim import lb, swimmers, tracers  # noqa: E402
+from lbswim.System import System  # noqa: E402
 
 
 def problem(size, nsw_total, ntr, arrays, seed=42):

@@ -87,14 +87,16 @@ def test_autotuned_tiles_keep_results():
 
 
 def test_fp32_ensemble_velocity_within_1e5_of_fp64():
+    # the batched FP32 members against the same solves in plain FP64 after
+    # 1000 steps: velocity-field relative L2 <= 1e-5
     from lbswim.ensemble import Ensemble
-    specs = SPECS[:4]
+    specs = SPECS
     batched = _build(specs)
     ens = Ensemble([(lat, sw, tr) for lat, sw, tr, _ in batched])
-    ens.Step(200)
+    ens.Step(1000)
     for b, spec in zip(batched, specs):
         ref = build_gpu(_case(*spec), "f64")
-        ref[3].Step(200)
+        ref[3].Step(1000)
         gs, rs = snapshot(*b[:3]), snapshot(*ref[:3])
         assert rel_l2(gs["u"], rs["u"]) < 1e-5
         assert rel_l2(gs["rho"], rs["rho"]) < 1e-6

@@ -1,20 +1,17 @@
 """The reference's own kernels build for the host from their sources and the
 oracle restatement agrees with them bit for bit on fresh seeded cases."""
-import os
-
 import numpy as np
 import pytest
 
+import build_ref
 import oracle as O
 
-REF = "/root/reference"
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lbswim")),
-                                reason="reference sources not present")
+REF = build_ref.reference_root()
+pytestmark = pytest.mark.skipif(REF is None, reason="reference sources not present")
 
 
 @pytest.fixture(scope="module")
 def ref_built():
-    import build_ref
     build_ref.build(REF, quiet=True)
     O._ref = None
     return True

@@ -1,8 +1,9 @@
 """lbswim_spread_forces_noalloc: the allocation-free spreading entry point.
 
-Callers that cannot allocate device memory (code under stream capture,
-real-time loops, hosts with their own allocator) pass their own device
-buffers; the scratch is the library's static device array.  Its result must
+Callers that cannot allocate device memory (plug-in code inside a host
+application that owns all device memory through its own allocator, real-time
+loops that cannot afford an allocation's implicit synchronisation) pass their
+own device buffers; the scratch is the library's static device array.  Its result must
 equal that of lbswim_swimmers_add_forces on the same swimmers, on two calls in
 a row (the second call finds the first call's leftovers in the scratch).
 This file is collected last so that a failure here stops a run only after
@@ -73,6 +74,16 @@ def test_noalloc_spread_rejects_sizes_beyond_its_limit():
     assert rc == -1 and b"limit" in _lib.lib.lbswim_last_error()
     rc = _lib.lib.lbswim_spread_forces_noalloc(
         C.c_void_p(r.data_ptr()), C.c_void_p(r.data_ptr()), 1, 1e-3, 0.5, 260, 260, 260,
+        C.c_void_p(force.data_ptr()), 0, None)
+    assert rc == -1 and b"limit" in _lib.lib.lbswim_last_error()
+    # a swimmer count that would wrap when doubled
+    rc = _lib.lib.lbswim_spread_forces_noalloc(
+        C.c_void_p(r.data_ptr()), C.c_void_p(r.data_ptr()), 2 ** 31 - 1, 1e-3, 0.5, 8, 8, 8,
+        C.c_void_p(force.data_ptr()), 0, None)
+    assert rc == -1 and b"limit" in _lib.lib.lbswim_last_error()
+    # few spread bins, but an axis beyond the gather's launch limits
+    rc = _lib.lib.lbswim_spread_forces_noalloc(
+        C.c_void_p(r.data_ptr()), C.c_void_p(r.data_ptr()), 1, 1e-3, 0.5, 4, 1000000, 4,
         C.c_void_p(force.data_ptr()), 0, None)
     assert rc == -1 and b"limit" in _lib.lib.lbswim_last_error()
     torch.cuda.synchronize()
