@@ -150,8 +150,14 @@ int lbswim_lattice_zero_force(lbswim_lattice* lat) {
   API_BEGIN
   check_lattice(lat);
   // Deferred: the next consumer of the force either overwrites it (spreading)
-  // or treats it as zero; a read of the field clears the buffer first.
-  lattice_zero_force(LAT(lat));
+  // or treats it as zero; a read of the field clears the buffer first.  With
+  // LBSWIM_COMPAT_EAGER_FIELDS an FP64 lattice clears its buffer at once.
+  Lattice* L = LAT(lat);
+  lattice_zero_force(L);
+  if ((L->compat & LBSWIM_COMPAT_EAGER_FIELDS) && L->precision == LBSWIM_F64) {
+    lattice_join(L);
+    lattice_zero_force_now(L);
+  }
   API_END
 }
 
@@ -223,7 +229,8 @@ int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags) {
   API_BEGIN
   check_lattice(lat);
   REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP |
-                      LBSWIM_COMPAT_EXACT_F64 | LBSWIM_COMPAT_WIDE_INDEX)) == 0,
+                      LBSWIM_COMPAT_EXACT_F64 | LBSWIM_COMPAT_WIDE_INDEX |
+                      LBSWIM_COMPAT_EAGER_FIELDS)) == 0,
           "unknown compat flag");
   LAT(lat)->compat = flags;
   API_END
@@ -697,6 +704,72 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
     else
       for (int i = 0; i < n_swimmers; ++i) swimmers_move(SW(swimmers[i]), L);
   }
+  API_END
+}
+
+// ---- storage and buffers of the C++ class API (include/liblbswim/) -------------
+int lbswim_device_alloc(size_t bytes, void** out) {
+  API_BEGIN
+  REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  LB_CUDA(cudaMalloc(out, bytes ? bytes : 16));
+  API_END
+}
+
+int lbswim_device_free(void* ptr) {
+  API_BEGIN
+  if (ptr) LB_CUDA(cudaFree(ptr));
+  API_END
+}
+
+int lbswim_memcpy_h2d(void* dst, const void* src, size_t bytes) {
+  API_BEGIN
+  REQUIRE(bytes == 0 || (dst && src), "NULL argument");
+  if (bytes) LB_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+  API_END
+}
+
+int lbswim_memcpy_d2h(void* dst, const void* src, size_t bytes) {
+  API_BEGIN_READ
+  REQUIRE(bytes == 0 || (dst && src), "NULL argument");
+  if (bytes) LB_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  API_END
+}
+
+int lbswim_lbparams_fill(lbswim_lbparams* p) {
+  API_BEGIN_READ
+  REQUIRE(p, "NULL argument");
+  fill_params(p, p->tau_s, p->tau_b);
+  API_END
+}
+
+int lbswim_lattice_device_buffers(const lbswim_lattice* lat, void* out[5]) {
+  API_BEGIN_READ
+  check_lattice(lat);
+  REQUIRE(out, "out is NULL");
+  const Lattice* L = CLAT(lat);
+  const bool packed = L->precision != LBSWIM_F64;
+  out[LBSWIM_FIELD_RHO] = packed ? (void*)L->hydro : L->rho;
+  out[LBSWIM_FIELD_U] = packed ? (void*)L->hydro : L->u;
+  out[LBSWIM_FIELD_FORCE] = L->force;
+  out[LBSWIM_FIELD_FOLD] = L->f[L->cur];
+  out[LBSWIM_FIELD_FNEW] = L->f[L->cur ^ 1];
+  API_END
+}
+
+int lbswim_swimmers_device_ptr(const lbswim_swimmers* sw, int field, void** out) {
+  API_BEGIN_READ
+  REQUIRE(sw && out, "NULL argument");
+  *out = sw_field(const_cast<Swimmers*>(reinterpret_cast<const Swimmers*>(sw)), field);
+  API_END
+}
+
+int lbswim_tracers_device_ptr(const lbswim_tracers* tr, int field, void** out) {
+  API_BEGIN_READ
+  REQUIRE(tr && out, "NULL argument");
+  REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
+  const Tracers* T = reinterpret_cast<const Tracers*>(tr);
+  *out = field == LBSWIM_TR_R ? T->r : (field == LBSWIM_TR_S ? T->s : T->v);
   API_END
 }
 

@@ -84,6 +84,12 @@ extern "C" {
  * overflow (15 * N >= 2^31 for the step, N >= 2^31 for the moves).  Batched
  * ensembles always use 32-bit offsets: their members are smaller. */
 #define LBSWIM_COMPAT_WIDE_INDEX 8
+/* FP64 lattices: ZeroForce clears the device force buffer at once instead of
+ * deferring it to the next consumer, so that every device buffer of the
+ * lattice holds its field as the reference's do (the reference's own kernels,
+ * or a user's, may then read or add to LatticeData's device arrays).  The C++
+ * class API of include/liblbswim/ sets it. */
+#define LBSWIM_COMPAT_EAGER_FIELDS 16
 
 typedef struct lbswim_lattice lbswim_lattice;
 typedef struct lbswim_swimmers lbswim_swimmers;
@@ -310,6 +316,30 @@ int lbswim_ensemble_autotune(lbswim_ensemble* ens);
 /* Slab shape of a lattice's step kernel: 0 = 8 x 32 cross-section, 1 = 16 x 16. */
 int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile);
 int lbswim_lattice_set_tile(lbswim_lattice* lat, int tile);
+
+/* ---- storage behind the C++ class API (include/liblbswim/) ------------------
+ * SharedArray<T>::SharedArray / ~SharedArray / H2D / D2H and the SharedItem
+ * equivalents (Shared.cu:4-59) for arrays that are not a library object's
+ * field: device memory, and synchronous copies between it and host memory. */
+int lbswim_device_alloc(size_t bytes, void** out);
+int lbswim_device_free(void* ptr);
+int lbswim_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int lbswim_memcpy_d2h(void* dst, const void* src, size_t bytes);
+/* LatticeEigenSet(LBParams*), d3q15.c:2-186: every table of p from the
+ * D3Q15 definitions; p->tau_s and p->tau_b are kept. */
+int lbswim_lbparams_fill(lbswim_lbparams* p);
+/* LatticeData::Device(), lb.cu:28-36 (LDView): the current device buffers of
+ * rho, u, force, fOld and fNew, indexed by LBSWIM_FIELD_*, without waiting for
+ * queued work (lbswim_lattice_device_ptr waits for it and documents the
+ * layouts).  fOld and fNew swap on every Step (lb.cu:241-244); the packed
+ * rho/u buffer of a reduced-precision lattice swaps on CalcHydro. */
+int lbswim_lattice_device_buffers(const lbswim_lattice* lat, void* out[5]);
+/* SwimmerArray::r/v/n.device (SwimmerArray.h:25-27): [3][n] doubles. */
+int lbswim_swimmers_device_ptr(const lbswim_swimmers* sw, int field, void** out);
+/* TracerArray::r/s/v.device (TracerArray.h:13-15): [3][n] doubles, in the
+ * library's binned work order (a permutation of the user's order, which the
+ * tracers' *_h2d / *_d2h translate). */
+int lbswim_tracers_device_ptr(const lbswim_tracers* tr, int field, void** out);
 
 /* ---- coupled step (System.Step, System.py:9-16) ---------------------------- */
 /* nsteps repetitions of: ZeroForce; AddForces for every swimmer array; Step;
