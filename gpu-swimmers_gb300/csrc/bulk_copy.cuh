@@ -1,0 +1,73 @@
+// bulk_copy.cuh -- one-dimensional bulk copies global -> shared memory
+// (cp.async.bulk, the TMA engine's untiled form) completed on an mbarrier.
+//
+// A copy moves a contiguous run of bytes; source and destination must be
+// 16-byte aligned and the size a multiple of 16.  The thread that arms a
+// barrier announces the bytes its copies will deliver (expect_tx); the barrier's
+// phase completes once they have all landed, and the threads that read the
+// buffer wait for that phase.  Every wait is bounded: past the limit it
+// records an error in the caller's flag and gives up, so a mistake in the
+// byte counts shows up as an error status instead of a hung GPU.
+#pragma once
+#include <cstdint>
+
+namespace lbswim {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+// Makes initialised barriers visible to the async proxy (before any copy uses them).
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Orders this thread's earlier generic-proxy accesses of shared memory before
+// later async-proxy writes (a bulk copy into a buffer the threads just read).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Wait for phase `parity` of the barrier; false (and *err set) past the limit.
+constexpr uint32_t MBAR_WAIT_LIMIT = 1u << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* err,
+                                          unsigned code) {
+  for (uint32_t i = 0; i < MBAR_WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicOr(err, code);
+  return false;
+}
+
+}  // namespace lbswim

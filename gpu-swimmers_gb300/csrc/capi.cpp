@@ -51,6 +51,15 @@ using namespace lbswim;
 
 static void check_lattice(const void* lat) { REQUIRE(lat, "lattice handle is NULL"); }
 
+// Uploaded particle positions and orientations must be finite: a NaN or an
+// infinity would otherwise travel through the moves' stencil arithmetic.  The
+// scan has no early exit so that it vectorises (it runs at memory speed).
+static void require_finite(const double* a, size_t n, const char* what) {
+  unsigned bad = 0;
+  for (size_t i = 0; i < n; ++i) bad |= !(std::fabs(a[i]) <= 1.7976931348623157e308);
+  if (bad) throw LbswimError{LBSWIM_EINVAL, std::string(what) + " holds a non-finite value"};
+}
+
 extern "C" {
 
 const char* lbswim_last_error(void) { return g_err.c_str(); }
@@ -230,9 +239,21 @@ int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags) {
   check_lattice(lat);
   REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP |
                       LBSWIM_COMPAT_EXACT_F64 | LBSWIM_COMPAT_WIDE_INDEX |
-                      LBSWIM_COMPAT_EAGER_FIELDS)) == 0,
+                      LBSWIM_COMPAT_EAGER_FIELDS | LBSWIM_COMPAT_NO_BULK_COPY)) == 0,
           "unknown compat flag");
   LAT(lat)->compat = flags;
+  API_END
+}
+
+int lbswim_lattice_get_status(lbswim_lattice* lat, unsigned* status, int clear) {
+  API_BEGIN_READ
+  check_lattice(lat);
+  REQUIRE(status, "status is NULL");
+  Lattice* L = LAT(lat);
+  lattice_join(L);
+  LB_CUDA(cudaMemcpyAsync(status, L->status, sizeof(unsigned), cudaMemcpyDeviceToHost, L->stream));
+  if (clear) LB_CUDA(cudaMemsetAsync(L->status, 0, sizeof(unsigned), L->stream));
+  LB_CUDA(cudaStreamSynchronize(L->stream));
   API_END
 }
 
@@ -403,6 +424,9 @@ int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host) {
   API_BEGIN
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
+  if (field == LBSWIM_SW_R || field == LBSWIM_SW_N)
+    require_finite(host, 3 * (size_t)W->n,
+                   field == LBSWIM_SW_R ? "swimmer positions" : "swimmer orientations");
   // the arrays are not bound to one stream: wait for the last kernel that used
   // them (on whichever stream), not for the whole device, and for the end
   // records a system step made of them after its move
@@ -535,6 +559,7 @@ int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host) {
   API_BEGIN
   REQUIRE(tr && host, "NULL argument");
   REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
+  if (field == LBSWIM_TR_R) require_finite(host, 3 * (size_t)TR(tr)->n, "tracer positions");
   tracers_h2d(TR(tr), field, host);
   API_END
 }

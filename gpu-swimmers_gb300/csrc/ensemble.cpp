@@ -179,6 +179,7 @@ static void build_tables(Ensemble* E) {
     M.bucket_count = L->spread.bucket_count;
     M.bucket_list = L->spread.bucket_list;
     M.max_abs_f = L->spread.max_abs_force;
+    M.status = L->status;
     M.nsw = nsw;
     if (W) {
       M.sw_r = W->r;

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_step_exact_f64(const double* __restrict
 // DoCalcHydro, lb.cu:250-295.
 __global__ void k_calc_hydro_exact_f64(const double* __restrict__ f, const double* __restrict__ F,
                                        double* __restrict__ rho, double* __restrict__ u,
-                                       long long N) {
+                                       long long N, unsigned* status) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
     double fo[15], mode[4];
@@ -142,6 +142,8 @@ __global__ void k_calc_hydro_exact_f64(const double* __restrict__ f, const doubl
       const double Fa = F ? F[a * N + s] : 0.0;
       u[a * N + s] = ddiv(dadd(mode[1 + a], dmul(0.5, Fa)), mode[0]);
     }
+    if (!finite_d(mode[0] + mode[1] + mode[2] + mode[3]))
+      raise_status(status, LBSWIM_STATUS_NONFINITE);
   }
 }
 
@@ -198,7 +200,7 @@ void exact_calc_hydro_f64(Lattice* L) {
   upload_tables(L->params);
   k_calc_hydro_exact_f64<<<grid_1d(L->n), 256, 0, L->stream>>>(
       (const double*)L->f[L->cur], L->force_zero_pending ? nullptr : (const double*)L->force,
-      (double*)L->rho, (double*)L->u, L->n);
+      (double*)L->rho, (double*)L->u, L->n, L->status);
   LB_CHECK_LAUNCH(1);
 }
 

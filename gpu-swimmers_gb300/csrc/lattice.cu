@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "bulk_copy.cuh"
 #include "lbswim_device.cuh"
 #include "lbswim_internal.h"
 #include "spread_slab.cuh"
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(256) k_step_push_f64(const double* __restrict_
 // rho, u from the stored distributions and the force, lb.cu:250-295.
 template <class S, class H>
 __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H* __restrict__ rho,
-                             H* __restrict__ u, long long N, H rho0) {
+                             H* __restrict__ u, long long N, H rho0, unsigned* status) {
   using T = H;
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
@@ -177,6 +178,7 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
     u[s] = (jx + T(0.5) * fx) / r;
     u[N + s] = (jy + T(0.5) * fy) / r;
     u[2 * N + s] = (jz + T(0.5) * fz) / r;
+    if (!finite_d((double)(r + jx + jy + jz))) raise_status(status, LBSWIM_STATUS_NONFINITE);
   }
 }
 
@@ -221,7 +223,8 @@ __global__ void k_init_from_hydro_packed(float4* __restrict__ packed, S* __restr
 // (CalcHydro of a reduced-precision lattice when the step's result is stale).
 template <class S>
 __global__ void k_calc_hydro_packed(const S* __restrict__ f, const float* __restrict__ F,
-                                    float4* __restrict__ hydro, long long N, float rho0) {
+                                    float4* __restrict__ hydro, long long N, float rho0,
+                                    unsigned* status) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N;
        s += (long long)gridDim.x * blockDim.x) {
     float d[15];
@@ -233,6 +236,7 @@ __global__ void k_calc_hydro_packed(const S* __restrict__ f, const float* __rest
     load_force(F, N, s, fx, fy, fz);
     const float inv = 1.0f / (rho0 + R);
     hydro[s] = make_float4((jx + 0.5f * fx) * inv, (jy + 0.5f * fy) * inv, (jz + 0.5f * fz) * inv, R);
+    if (!finite_f(R + jx + jy + jz)) raise_status(status, LBSWIM_STATUS_NONFINITE);
   }
 }
 
@@ -323,6 +327,7 @@ struct FusedArgs {
   float rho0;
   Relax<float> k;
   SlabEnds spread;  // pending dipole ends spread by the kernel itself (SPREAD instances)
+  unsigned* status;  // sticky error bits of the lattice (LBSWIM_STATUS_*)
 };
 
 // Post-collision populations 3-14 wait in shared memory until the output plane
@@ -355,6 +360,30 @@ constexpr int fused_smem_bytes() {
   return SPREAD ? SpreadLayout<TZ, TY, 1, spread_base<TZ, TY>()>::total
                 : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
+
+// Bulk-copy staging of the distributions (TMA instances, TZ = 32 and nz a
+// multiple of 32): the rows y0 - 1 .. y0 + TY of a plane are TY + 2 blocks of
+// 32 sites, each one contiguous run [15][32] of the blocked layout, copied by
+// one cp.async.bulk into a stage buffer; two stages, so that the next plane
+// lands while the current one is collided.  The sites just outside the
+// cross-section in z (z0 - 1 and z0 + 32) lie in other blocks and are still
+// loaded by their ring threads.
+constexpr int TMA_STAGES = 2;
+template <class S, int TY>
+constexpr int tma_row_bytes() { return 15 * 32 * (int)sizeof(S); }
+template <class S, int TY>
+constexpr int tma_stage_bytes() { return (TY + 2) * tma_row_bytes<S, TY>(); }
+template <class S, int TZ, int TY, bool SPREAD>
+constexpr int tma_stage_offset() { return (fused_smem_bytes<TZ, TY, SPREAD>() + 127) & ~127; }
+template <class S, int TZ, int TY, bool SPREAD>
+constexpr int tma_bar_offset() {
+  return tma_stage_offset<S, TZ, TY, SPREAD>() + TMA_STAGES * tma_stage_bytes<S, TY>();
+}
+template <class S, int TZ, int TY, bool SPREAD, bool TMA>
+constexpr int fused_smem_total() {
+  return TMA ? tma_bar_offset<S, TZ, TY, SPREAD>() + 8 * TMA_STAGES
+             : fused_smem_bytes<TZ, TY, SPREAD>();
+}
 // two CTAs per SM (1 KB of each CTA's shared memory is reserved) within 132 KB
 static_assert(2 * (fused_smem_bytes<32, 8, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
 static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
@@ -364,9 +393,12 @@ static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPRE
 // I is the site-index type: int when 15 N fits it (one multiply-add per
 // address), long long otherwise.
 // SPLIT: the form of the slab's force sums (slab_sums_split); SPREAD only.
-template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT>
+// TMA: the distributions of the cross-section's rows arrive by bulk copies
+// into shared memory (tma_* above); the lattice has nz a multiple of 32.
+template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT, bool TMA = false>
 __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
   static_assert(sizeof(S) < 8, "the fused step serves the reduced-precision layouts");
+  static_assert(!TMA || TZ == 32, "bulk-copied rows are whole 32-site blocks");
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
   constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
@@ -408,6 +440,40 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   const S* __restrict__ fo = (const S*)a.f_old;
   const float* __restrict__ F = a.force;
   const int my = ly * HZ + lz;
+  // TMA: this thread's site is in a bulk-copied row (all but the z halo)
+  const bool staged = TMA && active && lz >= 1 && lz <= ez;
+  S* stage = TMA ? reinterpret_cast<S*>(smraw + tma_stage_offset<S, TZ, TY, SPREAD>()) : nullptr;
+  uint64_t* bars =
+      TMA ? reinterpret_cast<uint64_t*>(smraw + tma_bar_offset<S, TZ, TY, SPREAD>()) : nullptr;
+  const int nrows = ey + 2;
+  // Thread 0 arms the stage's barrier and copies the rows of local plane k
+  // (x = x0 - 1 + k) into it.
+  auto issue = [&](int k) {
+    if constexpr (TMA) {
+      const int st = k & (TMA_STAGES - 1);
+      const int gx = wrap_once(x0 - 1 + k, nx);
+      constexpr uint32_t rb = tma_row_bytes<S, TY>();
+      mbar_arrive_expect_tx(bars + st, rb * (uint32_t)nrows);
+      const long long nzb = nz >> 5;
+      for (int r = 0; r < nrows; ++r) {
+        const int gyr = wrap_once(y0 + r - 1, ny);
+        const long long blk = ((long long)gx * ny + gyr) * nzb + tz;
+        bulk_g2s(stage + (size_t)(st * (TY + 2) + r) * (15 * 32), fo + blk * (15 * 32), rb,
+                 bars + st);
+      }
+    }
+  };
+  if constexpr (TMA) {
+    if (tid == 0) {
+      for (int st = 0; st < TMA_STAGES; ++st) mbar_init(bars + st, 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      issue(0);
+      if (ex + 2 > 1) issue(1);
+    }
+  }
 
   // ---- this slab's pending dipole ends and the fixed-point force plane ----
   SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>(), SPLIT> sp;
@@ -423,10 +489,11 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   float pre[18];
   auto load = [&](int gx) {
     const I s = (I)gx * nynz + yz;
+    if (!staged) {
+      const S* __restrict__ b = fo + fidx<S, I>(0, s, N);
 #pragma unroll
-    const S* __restrict__ b = fo + fidx<S, I>(0, s, N);
-#pragma unroll
-    for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(b + p * 32);
+      for (int p = 0; p < 15; ++p) pre[p] = Store<S>::ld(b + p * 32);
+    }
     if (F) {
       pre[15] = F[s];
       pre[16] = F[(N + s)];
@@ -446,6 +513,16 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
 #pragma unroll
     for (int i = 0; i < 18; ++i) cur[i] = pre[i];
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
+    if constexpr (TMA) {
+      // this plane's rows have landed in stage k % 2
+      const int st = k & (TMA_STAGES - 1);
+      mbar_wait(bars + st, (uint32_t)(k / TMA_STAGES) & 1u, a.status, LBSWIM_STATUS_COPY_TIMEOUT);
+      if (staged) {
+        const S* row = stage + (size_t)(st * (TY + 2) + ly) * (15 * 32) + (lz - 1);
+#pragma unroll
+        for (int p = 0; p < 15; ++p) cur[p] = Store<S>::ld(row + p * 32);
+      }
+    }
     if (SPREAD && active) {
       // force = base + spread (k_force_slab writes the same bits)
 #pragma unroll
@@ -474,6 +551,13 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       new2 = d[2];
     }
     __syncthreads();
+    if constexpr (TMA) {
+      // every thread has read stage k % 2: it takes plane k + 2
+      if (tid == 0 && k + TMA_STAGES < ex + 2) {
+        fence_proxy_async_smem();
+        issue(k + TMA_STAGES);
+      }
+    }
     if (SPREAD && k + 1 < ex + 2) sp.scatter(k + 1, rt, blockDim.x);
     if (k >= 2 && interior) {
       // output plane x = x0 + k - 2 pulls A of plane x-1, B of x, C of x+1
@@ -495,6 +579,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       }
       float R, jx, jy, jz;
       hydro_moments(g, R, jx, jy, jz);
+      if (!finite_f(R + jx + jy + jz)) raise_status(a.status, LBSWIM_STATUS_NONFINITE);
       S* __restrict__ fn = (S*)a.f_new;
 #pragma unroll
       S* __restrict__ bo = fn + fidx<S, I>(0, s, N);
@@ -517,13 +602,13 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   }
 }
 
-template <class S, int TZ, int TY, bool SPREAD, class I>
+template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
   const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (!SPREAD || slab_sums_split(a.spread, slab, a.nx, a.ny, a.nz))
-    fused_slab<S, TZ, TY, SPREAD, I, true>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
+    fused_slab<S, TZ, TY, SPREAD, I, true, TMA>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
   else
-    fused_slab<S, TZ, TY, SPREAD, I, false>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
+    fused_slab<S, TZ, TY, SPREAD, I, false, TMA>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,6 +662,7 @@ __global__ void __launch_bounds__(8 * 32 + FUSED_RING_THREADS, 2) k_ens_step(Ens
     a.k = Relax<float>{M.omega_s, M.omega_b, M.force_s, M.force_b};
     a.spread = SlabEnds{(const EndRecord<float>*)M.ends, M.bucket_count, M.bucket_list,
                         2 * M.nsw, M.max_abs_f};
+    a.status = M.status;
     // members have few enough swimmers for split force sums on every slab
     // (checked when the members are set)
     if (M.tile == 1)
@@ -704,6 +790,8 @@ void lattice_alloc(Lattice* L) {
     LB_CUDA(cudaMemsetAsync(L->hydro, 0, N * sizeof(float4), L->stream));
   }
   L->force = dmalloc(3 * N * he);
+  L->status = (unsigned*)dmalloc(256);
+  LB_CUDA(cudaMemsetAsync(L->status, 0, 256, L->stream));
   // Contents start at zero so that reading a field before setting it is defined.
   LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * N * he, L->stream));
   LB_CUDA(cudaMemsetAsync(L->f[0], 0, fbytes, L->stream));
@@ -712,7 +800,7 @@ void lattice_alloc(Lattice* L) {
 
 void lattice_free(Lattice* L) {
   void* ptrs[] = {L->f[0], L->f[1], L->rho, L->u, L->hydro, L->hydro_shadow, L->force,
-                  L->staging};
+                  L->staging, L->status};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   spread_free(L->spread);
@@ -869,17 +957,24 @@ void lattice_init_from_hydro(Lattice* L) {
   L->f_version++;
 }
 
-template <class S, int TZ, int TY, bool SPREAD, class I>
+template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA>
 static void launch_fused_i(Lattice* L, const FusedArgs& a) {
-  constexpr int smem = fused_smem_bytes<TZ, TY, SPREAD>();
+  constexpr int smem = fused_smem_total<S, TZ, TY, SPREAD, TMA>();
   static bool configured = false;  // per template instance, per process
   if (!configured) {
-    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I>,
+    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    // the bulk-copied rows bypass L1: give shared memory the whole carveout so
+    // that two CTAs fit an SM
+    if (TMA)
+      LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA>,
+                                   cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared));
     configured = true;
   }
   dim3 grid((a.nz + TZ - 1) / TZ, (a.ny + TY - 1) / TY, (a.nx + FUSED_LX - 1) / FUSED_LX);
-  k_fused_step<S, TZ, TY, SPREAD, I><<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
+  k_fused_step<S, TZ, TY, SPREAD, I, TMA>
+      <<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
   LB_CHECK_LAUNCH(1);
 }
 
@@ -887,12 +982,28 @@ static void launch_fused_i(Lattice* L, const FusedArgs& a) {
 // reduced-precision buffers hold 15 f_sites(n) values).
 inline bool fits_int_index(long long n) { return 15 * ((n + 31) & ~31ll) < (1ll << 31); }
 
+// Rows of whole 32-site blocks are bulk-copied when the cross-section is 32
+// sites wide and nz a multiple of 32 (each row of the slab is then one block).
+inline bool fused_uses_tma(const Lattice* L, int TZ) {
+  return TZ == 32 && (L->size[2] & 31) == 0 && !(L->compat & LBSWIM_COMPAT_NO_BULK_COPY);
+}
+
 template <class S, int TZ, int TY, bool SPREAD>
 static void launch_fused(Lattice* L, const FusedArgs& a) {
-  if (fits_int_index(a.n) && !(L->compat & LBSWIM_COMPAT_WIDE_INDEX))
-    launch_fused_i<S, TZ, TY, SPREAD, int>(L, a);
+  const bool wide = !fits_int_index(a.n) || (L->compat & LBSWIM_COMPAT_WIDE_INDEX);
+  if constexpr (TZ == 32) {
+    if (fused_uses_tma(L, TZ)) {
+      if (wide)
+        launch_fused_i<S, TZ, TY, SPREAD, long long, true>(L, a);
+      else
+        launch_fused_i<S, TZ, TY, SPREAD, int, true>(L, a);
+      return;
+    }
+  }
+  if (wide)
+    launch_fused_i<S, TZ, TY, SPREAD, long long, false>(L, a);
   else
-    launch_fused_i<S, TZ, TY, SPREAD, long long>(L, a);
+    launch_fused_i<S, TZ, TY, SPREAD, int, false>(L, a);
 }
 
 // Pending dipole ends are spread by the step kernel itself (true), or first
@@ -932,6 +1043,7 @@ static void fused_step_t(Lattice* L) {
   a.n = L->n;
   a.rho0 = (float)L->rho0;
   a.k = make_relax<float>(L->tau_s, L->tau_b);
+  a.status = L->status;
   if (L->fused_tile == 1)
     fused_step_tile<S, 16, 16>(L, a);
   else
@@ -1021,11 +1133,11 @@ static void calc_hydro_t(Lattice* L) {
   if (L->precision == LBSWIM_F64)
     k_calc_hydro<double, double><<<grid_for(N, 256), 256, 0, L->stream>>>(
         (const double*)L->f[L->cur], L->force_zero_pending ? nullptr : (const double*)L->force,
-        (double*)L->rho, (double*)L->u, N, 0.0);
+        (double*)L->rho, (double*)L->u, N, 0.0, L->status);
   else
     k_calc_hydro_packed<S><<<grid_for(N, 256), 256, 0, L->stream>>>(
         (const S*)L->f[L->cur], L->force_zero_pending ? nullptr : (const float*)L->force,
-        L->hydro, N, (float)L->rho0);
+        L->hydro, N, (float)L->rho0, L->status);
   LB_CHECK_LAUNCH(1);
 }
 

@@ -395,6 +395,18 @@ __device__ __forceinline__ void rng_normal3(uint64_t seed, uint32_t swimmer, uin
   g[2] = __dmul_rn(r2, c4);
 }
 
+// ---- sticky status bits (LBSWIM_STATUS_* of lbswim_c.h) ---------------------
+// x is finite (false for NaN and +-inf).
+__device__ __forceinline__ bool finite_f(float x) { return fabsf(x) < __int_as_float(0x7f800000); }
+__device__ __forceinline__ bool finite_d(double x) {
+  return fabs(x) < __longlong_as_double(0x7ff0000000000000ll);
+}
+__device__ __forceinline__ void raise_status(unsigned* status, unsigned bit) {
+  if (status) atomicOr(status, bit);
+}
+// A moved particle's new coordinate must lie in [0, n) (false for NaN).
+__device__ __forceinline__ bool in_box(double x, int n) { return x >= 0.0 && x < (double)n; }
+
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 __device__ __forceinline__ int wrap_any(int i, int n) {

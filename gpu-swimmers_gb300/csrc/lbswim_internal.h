@@ -128,6 +128,7 @@ struct Lattice {
   float4* hydro = nullptr;
   float4* hydro_shadow = nullptr;
   void* force = nullptr;
+  unsigned* status = nullptr;  // device: sticky LBSWIM_STATUS_* bits
   cudaStream_t stream = 0;
   int time_step = 0;
   int compat = LBSWIM_COMPAT_INIT_SXZ;
@@ -225,6 +226,7 @@ struct EnsMember {
   double* tr_r;
   double* tr_s;
   double* tr_v;
+  unsigned* status;  // the member lattice's sticky status bits
 };
 
 // Device tables of an ensemble; the batched kernels of a captured step read

@@ -643,7 +643,7 @@ template <class U, class T>
 __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __restrict__ swv,
                                 double* __restrict__ swn, lbswim_common_params c,
                                 unsigned long long seed, unsigned long long step, Dims D,
-                                const U* __restrict__ u) {
+                                const U* __restrict__ u, unsigned* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nsw) return;
   double r[3], n0[3];
@@ -659,7 +659,9 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     if (!c.translational_advection_off) rDot = __dadd_rn(rDot, (double)v[d]);
     rMinus[d] = __dsub_rn(r[d], __dmul_rn(n0[d], c.l));
     swv[nsw * d + i] = rDot;
-    swr[nsw * d + i] = wrap_position<T>(r[d] + rDot, D.n[d]);
+    const double rn = wrap_position<T>(r[d] + rDot, D.n[d]);
+    swr[nsw * d + i] = rn;
+    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
   }
   const float rnd = rng_uniform(seed, (uint32_t)i, step);
   double nn[3];
@@ -680,7 +682,8 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
 // DoTracerArrayMove, TracerArray.cu:12-43 (s accumulated per tracer).
 template <class U, class T>
 __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restrict__ s,
-                               double* __restrict__ v, Dims D, const U* __restrict__ u) {
+                               double* __restrict__ v, Dims D, const U* __restrict__ u,
+                               unsigned* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ntr) return;
   double rr[3], ss[3];
@@ -693,8 +696,10 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
   for (int d = 0; d < 3; ++d) {
     const double vd = (double)vv[d];
     v[ntr * d + i] = vd;
-    r[ntr * d + i] = wrap_position<T>(rr[d] + vd, D.n[d]);
+    const double rn = wrap_position<T>(rr[d] + vd, D.n[d]);
+    r[ntr * d + i] = rn;
     s[ntr * d + i] = ss[d] + vd;
+    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
   }
 }
 
@@ -1001,7 +1006,8 @@ template <class I = int>
 __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __restrict__ r,
                                                    double* __restrict__ s,
                                                    double* __restrict__ v, Dims D,
-                                                   const float4* __restrict__ h) {
+                                                   const float4* __restrict__ h,
+                                                   unsigned* status) {
   __shared__ StencilSet<TRACER_MOVE_BLOCK> st;
   __shared__ float3 vel[TRACER_MOVE_BLOCK];
   const int i = blk * TRACER_MOVE_BLOCK + threadIdx.x;
@@ -1026,16 +1032,18 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
   for (int d = 0; d < 3; ++d) {
     const double vd = f2d_exact(vv[d]);
     v[(long long)ntr * d + i] = vd;
-    r[(long long)ntr * d + i] = advance_position(rr[d], vv[d], D.n[d]);
+    const double rn = advance_position(rr[d], vv[d], D.n[d]);
+    r[(long long)ntr * d + i] = rn;
     s[(long long)ntr * d + i] = ss[d] + vd;
+    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
   }
 }
 
 template <class I>
 __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_tracers_move_f32(
     int ntr, double* __restrict__ r, double* __restrict__ s, double* __restrict__ v, Dims D,
-    const float4* __restrict__ h) {
-  tracers_move_block<I>(blockIdx.x, ntr, r, s, v, D, h);
+    const float4* __restrict__ h, unsigned* status) {
+  tracers_move_block<I>(blockIdx.x, ntr, r, s, v, D, h, status);
 }
 
 // A block takes SWIMMERS_PER_BLOCK swimmers: two stencils (front and rear
@@ -1048,7 +1056,7 @@ template <class I = int>
 __device__ __forceinline__ void swimmers_move_block(
     int blk, int nsw, double* __restrict__ swr, double* __restrict__ swv,
     double* __restrict__ swn, lbswim_common_params c, unsigned long long seed,
-    unsigned long long step, Dims D, const float4* __restrict__ h) {
+    unsigned long long step, Dims D, const float4* __restrict__ h, unsigned* status) {
   constexpr int B = SWIMMERS_PER_BLOCK;
   // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
   __shared__ StencilSet<2 * B> st;
@@ -1089,7 +1097,9 @@ __device__ __forceinline__ void swimmers_move_block(
     float rDot = mP * n0[d];
     if (!c.translational_advection_off) rDot += v[d];
     swv[nsw * d + i] = f2d_exact(rDot);
-    swr[nsw * d + i] = advance_position(r[d], rDot, D.n[d]);
+    const double rn = advance_position(r[d], rDot, D.n[d]);
+    swr[nsw * d + i] = rn;
+    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
   }
   if (tumble) {
     float nn[3];
@@ -1116,8 +1126,8 @@ template <class I>
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
     lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
-    const float4* __restrict__ h) {
-  swimmers_move_block<I>(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h);
+    const float4* __restrict__ h, unsigned* status) {
+  swimmers_move_block<I>(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h, status);
 }
 
 // ---- batched ensembles: per-step reset, end records, moves --------------------
@@ -1190,12 +1200,12 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_ens_move(EnsTable t, int 
       const int m = ens_find(t.sw_prefix, nmem, vb);
       const EnsMember& M = t.mem[m];
       swimmers_move_block(vb - t.sw_prefix[m], M.nsw, M.sw_r, M.sw_v, M.sw_n, M.common, M.seed,
-                          M.step0 + g, ens_dims(M), (const float4*)M.hyd[parity]);
+                          M.step0 + g, ens_dims(M), (const float4*)M.hyd[parity], M.status);
     } else {
       const int m = ens_find(t.tr_prefix, nmem, vb - nsb);
       const EnsMember& M = t.mem[m];
       tracers_move_block(vb - nsb - t.tr_prefix[m], M.ntr, M.tr_r, M.tr_s, M.tr_v, ens_dims(M),
-                         (const float4*)M.hyd[parity]);
+                         (const float4*)M.hyd[parity], M.status);
     }
     __syncthreads();
   }
@@ -1504,15 +1514,18 @@ void swimmers_move(Swimmers* W, Lattice* L) {
     const int grid = (W->n + 255) / 256;
     if (L->precision == LBSWIM_F64)
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
-          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u);
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u,
+          L->status);
     else if (wide_particle_index(L))
       k_swimmers_move_f32<long long><<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
                                        SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
-          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro,
+          L->status);
     else
       k_swimmers_move_f32<int><<<(W->n + SWIMMERS_PER_BLOCK - 1) / SWIMMERS_PER_BLOCK,
                                  SWIMMER_MOVE_BLOCK, 0, L->stream>>>(
-          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro);
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const float4*)L->hydro,
+          L->status);
     LB_CHECK_LAUNCH(1);
     swimmers_mark(W, L->stream);
   }
@@ -1756,15 +1769,15 @@ static void tracers_move_on(Tracers* T, Lattice* L, cudaStream_t stream) {
   const int grid = (T->n + 255) / 256;
   if (L->precision == LBSWIM_F64)
     k_tracers_move<double, double><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
-                                                                 (const double*)L->u);
+                                                                 (const double*)L->u, L->status);
   else if (wide_particle_index(L))
     k_tracers_move_f32<long long><<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK,
                                     TRACER_MOVE_BLOCK, 0, stream>>>(T->n, T->r, T->s, T->v, D,
-                                                                    L->hydro);
+                                                                    L->hydro, L->status);
   else
     k_tracers_move_f32<int><<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK,
                               TRACER_MOVE_BLOCK, 0, stream>>>(T->n, T->r, T->s, T->v, D,
-                                                              L->hydro);
+                                                              L->hydro, L->status);
   LB_CHECK_LAUNCH(1);
 }
 

@@ -23,6 +23,8 @@ FIELD_COMPONENTS = {FIELD_RHO: 1, FIELD_U: 3, FIELD_FORCE: 3, FIELD_FOLD: 15, FI
 SW_R, SW_V, SW_N = 0, 1, 2
 TR_R, TR_S, TR_V = 0, 1, 2
 COMPAT_INIT_SXZ, COMPAT_SYNC_STEP, COMPAT_EXACT_F64, COMPAT_WIDE_INDEX = 1, 2, 4, 8
+COMPAT_EAGER_FIELDS, COMPAT_NO_BULK_COPY = 16, 32
+STATUS_NONFINITE, STATUS_PARTICLE_OUTSIDE, STATUS_COPY_TIMEOUT = 1, 2, 4
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",
           -5: "not supported"}
@@ -121,6 +123,15 @@ _PROTOS = {
     "lbswim_tracers_d2h": (C.c_int, [_VP, C.c_int, _D]),
     "lbswim_system_step": (C.c_int, [_VP, C.POINTER(_VP), C.c_int, C.POINTER(_VP), C.c_int,
                                      C.c_int]),
+    "lbswim_lattice_get_status": (C.c_int, [_VP, C.POINTER(C.c_uint), C.c_int]),
+    "lbswim_device_alloc": (C.c_int, [C.c_size_t, C.POINTER(_VP)]),
+    "lbswim_device_free": (C.c_int, [_VP]),
+    "lbswim_memcpy_h2d": (C.c_int, [_VP, _VP, C.c_size_t]),
+    "lbswim_memcpy_d2h": (C.c_int, [_VP, _VP, C.c_size_t]),
+    "lbswim_lbparams_fill": (C.c_int, [C.POINTER(LBParamsStruct)]),
+    "lbswim_lattice_device_buffers": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "lbswim_swimmers_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP)]),
+    "lbswim_tracers_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP)]),
 }
 
 

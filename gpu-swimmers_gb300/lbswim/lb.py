@@ -216,6 +216,14 @@ class Lattice:
         _lib.check(_lib.lib.lbswim_lattice_set_tau(self._h, float(tau_s), float(tau_b)))
         self._params = None
 
+    def status(self, clear=False):
+        """Sticky status bits the lattice's kernels and the particle moves on it
+        set (_lib.STATUS_NONFINITE, STATUS_PARTICLE_OUTSIDE, STATUS_COPY_TIMEOUT);
+        waits for the lattice's queued work; clear resets them."""
+        out = C.c_uint()
+        _lib.check(_lib.lib.lbswim_lattice_get_status(self._h, C.byref(out), int(bool(clear))))
+        return out.value
+
     def conservation(self):
         """(mass, momentum x, y, z): sums of f and c f over the lattice in FP64,
         in a fixed order."""

@@ -90,6 +90,18 @@ extern "C" {
  * or a user's, may then read or add to LatticeData's device arrays).  The C++
  * class API of include/liblbswim/ sets it. */
 #define LBSWIM_COMPAT_EAGER_FIELDS 16
+/* FP32/BF16/FP16 lattices: the step kernel loads every site's distributions
+ * with per-thread loads instead of bulk-copying whole rows into shared memory
+ * (which it does when nz is a multiple of 32); the results are the same bits. */
+#define LBSWIM_COMPAT_NO_BULK_COPY 32
+
+/* ---- sticky status bits (lbswim_lattice_get_status) ----------------------- */
+/* No reference counterpart (the reference checks no kernel).  Kernels of a
+ * lattice, and of the particles moved with it, set these bits in a status
+ * word on the device; they stay set until read with clear != 0. */
+#define LBSWIM_STATUS_NONFINITE 1        /* a step or CalcHydro gave a non-finite rho or u */
+#define LBSWIM_STATUS_PARTICLE_OUTSIDE 2 /* a move left a particle non-finite or outside the box */
+#define LBSWIM_STATUS_COPY_TIMEOUT 4     /* a kernel gave up waiting for its own bulk copies */
 
 typedef struct lbswim_lattice lbswim_lattice;
 typedef struct lbswim_swimmers lbswim_swimmers;
@@ -169,6 +181,10 @@ int lbswim_lattice_get_precision(const lbswim_lattice* lat, int* out);
  * sum_p f_p and sum_p c_p f_p, accumulated in FP64 in a fixed order (the same
  * bits every call), for conservation checks. */
 int lbswim_lattice_conservation(lbswim_lattice* lat, double out[4]);
+/* No reference counterpart: the sticky status bits (LBSWIM_STATUS_*) that
+ * this lattice's kernels and the moves of particles on it have set; waits
+ * for the lattice's queued work first, and clears them when clear != 0. */
+int lbswim_lattice_get_status(lbswim_lattice* lat, unsigned* status, int clear);
 /* No reference counterpart: behaviour switches and stream binding. */
 int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags);
 int lbswim_lattice_set_stream(lbswim_lattice* lat, void* cuda_stream);
@@ -209,7 +225,8 @@ int lbswim_swimmers_get_num(const lbswim_swimmers* sw, int* out);
 int lbswim_swimmers_add_forces(lbswim_swimmers* sw, lbswim_lattice* lat);
 /* SwimmerArray::Move, SwimmerArray.cu:212-220. */
 int lbswim_swimmers_move(lbswim_swimmers* sw, lbswim_lattice* lat);
-/* SharedArray<double>::H2D / D2H of r, v or n (3*n doubles). */
+/* SharedArray<double>::H2D / D2H of r, v or n (3*n doubles).  Positions and
+ * orientations must be finite (else LBSWIM_EINVAL, nothing copied). */
 int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host);
 int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host);
 /* No reference counterpart: the D2H of r, v and n (any may be NULL) with one
@@ -273,6 +290,7 @@ int lbswim_tracers_destroy(lbswim_tracers* tr);
 int lbswim_tracers_get_num(const lbswim_tracers* tr, int* out);
 /* TracerArray::Move, TracerArray.cu:45-52. */
 int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat);
+/* Positions must be finite (else LBSWIM_EINVAL, nothing copied). */
 int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host);
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
 

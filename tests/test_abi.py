@@ -83,3 +83,17 @@ def test_c_program_builds_against_header_and_library(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(exe)
+
+
+def test_lbparams_fill_matches_oracle_tables():
+    # LatticeEigenSet of the C++ class API (d3q15.c:2-186) runs on the host
+    import numpy as np
+    import oracle as O
+    from lbswim import _lib
+    p = _lib.LBParamsStruct()
+    p.tau_s, p.tau_b = 0.7, 1.3
+    _lib.check(_lib.lib.lbswim_lbparams_fill(C.byref(p)))
+    ref = O.params_dict(O.params(0.7, 1.3))
+    assert (p.tau_s, p.tau_b) == (0.7, 1.3)
+    for name in ("w", "xi", "ci", "Q", "complement", "norms", "mm", "mmi"):
+        assert np.array_equal(np.ctypeslib.as_array(getattr(p, name)), ref[name]), name
