@@ -392,6 +392,8 @@ def our_arm(args, world, rank, local):
     # step leaves idle.
     stream = torch.cuda.Stream(priority=-5)
     lat.set_stream(stream.cuda_stream)
+    if args.no_bulk_copy:
+        lat.set_compat(_lib.COMPAT_INIT_SXZ | _lib.COMPAT_NO_BULK_COPY)
     upload(case, lat, sw, tr)
 
     def barrier():
@@ -602,6 +604,8 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f64", "f32", "bf16", "f16"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-bulk-copy", action="store_true",
+                    help="step kernel with per-thread loads only (comparison runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="timed CPU work of the cpu_baseline leg")
     ap.add_argument("--f64-steps", type=int, default=20,

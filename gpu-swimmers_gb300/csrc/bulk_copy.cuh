@@ -5,9 +5,9 @@
 // 16-byte aligned and the size a multiple of 16.  The thread that arms a
 // barrier announces the bytes its copies will deliver (expect_tx); the barrier's
 // phase completes once they have all landed, and the threads that read the
-// buffer wait for that phase.  Every wait is bounded: past the limit it
-// records an error in the caller's flag and gives up, so a mistake in the
-// byte counts shows up as an error status instead of a hung GPU.
+// buffer wait for that phase.  Every wait is bounded in time: past the limit
+// it records an error in the caller's status word and gives up, so a mistake
+// in the byte counts shows up as an error status instead of a hung GPU.
 #pragma once
 #include <cstdint>
 
@@ -60,14 +60,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Wait for phase `parity` of the barrier; false (and *err set) past the limit.
-constexpr uint32_t MBAR_WAIT_LIMIT = 1u << 24;
+// Wait for phase `parity` of the barrier.  The wait is bounded by time
+// (MBAR_WAIT_NS of the global timer): past it, the bit `code` is set in *err
+// and the wait returns false.  Once that bit is set, later waits of any CTA
+// return at once, so a kernel whose copies never complete still ends within
+// about one limit (its results are then wrong, and the status says so).
+constexpr unsigned long long MBAR_WAIT_NS = 2000000000ull;  // 2 s
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* err,
                                           unsigned code) {
-  for (uint32_t i = 0; i < MBAR_WAIT_LIMIT; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
-  if (err) atomicOr(err, code);
-  return false;
+    if (err && (*(volatile unsigned*)err & code)) return false;
+    if (global_ns() - t0 > MBAR_WAIT_NS) {
+      if (err) atomicOr(err, code);
+      return false;
+    }
+  }
 }
 
 }  // namespace lbswim

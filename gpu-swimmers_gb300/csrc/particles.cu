@@ -328,7 +328,7 @@ __device__ __forceinline__ void end_records_block(
     int blk, int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P,
     double l, Dims D, EndRecord<T>* __restrict__ ends, int e_base,
     unsigned* __restrict__ max_abs_f, TileGrid G, unsigned* __restrict__ bucket_count,
-    int* __restrict__ bucket_list) {
+    int* __restrict__ bucket_list, unsigned long long* __restrict__ endvel = nullptr) {
   __shared__ EndRecord<T> srec[REC_THREADS];
   __shared__ unsigned smax;
   if (threadIdx.x == 0) smax = 0u;
@@ -370,6 +370,9 @@ __device__ __forceinline__ void end_records_block(
     }
     mbits = __float_as_uint(m);
     if (bucket_count) bucket_end(e_base + e, rec.o, D, G, bucket_count, bucket_list);
+    // the velocity sums the next step kernel adds to start at zero
+    if (endvel)
+      for (int c = 0; c < 3; ++c) endvel[3ll * (e_base + e) + c] = 0ull;
   }
   // non-negative floats order like their bit patterns: a warp's largest, then
   // one shared-memory atomic per warp
@@ -388,9 +391,10 @@ template <class T>
 __global__ void __launch_bounds__(REC_THREADS) k_end_records(
     int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P, double l,
     Dims D, EndRecord<T>* __restrict__ ends, int e_base, unsigned* __restrict__ max_abs_f,
-    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list) {
+    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list,
+    unsigned long long* __restrict__ endvel) {
   end_records_block<T>(blockIdx.x, nsw, r, nv, P, l, D, ends, e_base, max_abs_f, G, bucket_count,
-                       bucket_list);
+                       bucket_list, endvel);
 }
 
 // Slab buckets of recorded ends (the slab shape changed since they were recorded).
@@ -999,6 +1003,68 @@ __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const
   }
 }
 
+// The swimmers' interpolation in fixed point (vel_quant): lane `sub` of the L
+// lanes of a point takes z node sub & 3 and y nodes sub >> 2, sub >> 2 + L/4,
+// ..., over the x planes of the stencil -- its four nodes, or for nx < 4 the
+// planes the nodes fold onto, with their summed weights (axis_weight), as the
+// step kernel's plane-by-plane gather sees them -- so that the sums equal the
+// step kernel's bit for bit.
+template <int L, int NP, class I = int>
+__device__ __forceinline__ void gather_point_fixed(const float4* __restrict__ h, const Dims& D,
+                                                   const StencilSet<NP>& s, int p, int sub,
+                                                   long long& ax, long long& ay, long long& az) {
+  ax = ay = az = 0;
+  if (!s.active[p]) return;
+  const int nx = D.n[0], nz = D.n[2];
+  const I nynz = (I)D.n[1] * nz;
+  const int kz = sub & 3;
+  const int z = node_after(s.o[2][p], kz, nz);
+  const float pz = s.w[2][kz][p];
+  const int np = nx >= 4 ? 4 : nx;
+  I xo[4];
+  float wx[4];
+  float phx[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) phx[i] = s.w[0][i][p];
+#pragma unroll
+  for (int ix = 0; ix < 4; ++ix) {
+    const int gx = nx >= 4 ? node_after(s.o[0][p], ix, nx) : ix;
+    xo[ix] = (I)gx * nynz;
+    wx[ix] = nx >= 4 ? phx[ix] : (ix < nx ? axis_weight(ix, s.o[0][p], nx, phx) : 0.f);
+  }
+#pragma unroll
+  for (int jy = sub >> 2; jy < 4; jy += L / 4) {
+    const I yz = (I)node_after(s.o[1][p], jy, D.n[1]) * nz + z;
+    const float py = s.w[1][jy][p];
+#pragma unroll
+    for (int ix = 0; ix < 4; ++ix) {
+      if (ix >= np) break;
+      const float4 q = __ldg(h + xo[ix] + yz);
+      ax += vel_quant(node_contrib(py, pz, wx[ix], q.x));
+      ay += vel_quant(node_contrib(py, pz, wx[ix], q.y));
+      az += vel_quant(node_contrib(py, pz, wx[ix], q.z));
+    }
+  }
+}
+
+template <int L, int NP, class I = int>
+__device__ __forceinline__ void gather_block_fixed(const float4* __restrict__ h, const Dims& D,
+                                                   const StencilSet<NP>& st, float3* vel) {
+  const int sub = threadIdx.x & (L - 1);
+  const int groups = blockDim.x / L;
+  for (int p = threadIdx.x / L; p < NP; p += groups) {
+    long long ax, ay, az;
+    gather_point_fixed<L, NP, I>(h, D, st, p, sub, ax, ay, az);
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, off);
+      ay += __shfl_xor_sync(0xffffffffu, ay, off);
+      az += __shfl_xor_sync(0xffffffffu, az, off);
+    }
+    if (sub == 0) vel[p] = make_float3(vel_value(ax), vel_value(ay), vel_value(az));
+  }
+}
+
 constexpr int TRACER_MOVE_BLOCK = 256;
 constexpr int TRACER_LANES = 4;  // lanes per interpolation point
 
@@ -1052,49 +1118,21 @@ constexpr int SWIMMERS_PER_BLOCK = 64;
 constexpr int SWIMMER_LANES = 4;  // lanes per interpolation point
 constexpr int SWIMMER_MOVE_BLOCK = SWIMMERS_PER_BLOCK * SWIMMER_LANES;
 
-template <class I = int>
-__device__ __forceinline__ void swimmers_move_block(
-    int blk, int nsw, double* __restrict__ swr, double* __restrict__ swv,
-    double* __restrict__ swn, lbswim_common_params c, unsigned long long seed,
-    unsigned long long step, Dims D, const float4* __restrict__ h, unsigned* status) {
-  constexpr int B = SWIMMERS_PER_BLOCK;
-  // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
-  __shared__ StencilSet<2 * B> st;
-  __shared__ float3 vel[2 * B];
-  const int t = threadIdx.x, i = blk * B + t;
-  const bool mine = t < B, valid = mine && i < nsw;
-  double r[3] = {0.0, 0.0, 0.0}, nd[3] = {0.0, 0.0, 0.0};
-  float n0[3] = {0.f, 0.f, 0.f};
-  bool tumble = false, rotate = false;
-  if (valid) {
-    double rMinus[3];
-    for (int d = 0; d < 3; ++d) {
-      r[d] = swr[nsw * d + i];
-      nd[d] = swn[nsw * d + i];
-      n0[d] = (float)nd[d];
-    }
-    tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
-    rotate = !tumble && !c.rotational_advection_off;
-    point_stencil(D, r, st, t);
-    if (rotate) {
-      for (int d = 0; d < 3; ++d) rMinus[d] = r[d] - nd[d] * c.l;
-      point_stencil(D, rMinus, st, B + t);
-    } else {
-      st.active[B + t] = 0;
-    }
-  } else if (mine) {
-    st.active[t] = 0;
-    st.active[B + t] = 0;
-  }
-  __syncthreads();
-  gather_block<SWIMMER_LANES, 2 * SWIMMERS_PER_BLOCK, I>(h, D, st, vel);
-  __syncthreads();
-  if (!valid) return;
-  const float3 w = vel[t], wm = vel[B + t];
-  const float v[3] = {w.x, w.y, w.z}, vm[3] = {wm.x, wm.y, wm.z};
+// The update of swimmer i from the fluid velocity at its front point r (v)
+// and at its rear point r - l n (vm): SwimmerArray.cu:151-209, with the FP32
+// path's arithmetic (Q44 positions, FP32 turn added to the FP64 orientation,
+// FP32 tumble normals).
+__device__ __forceinline__ void swimmer_update(int i, int nsw, double* __restrict__ swr,
+                                               double* __restrict__ swv, double* __restrict__ swn,
+                                               const lbswim_common_params& c,
+                                               unsigned long long seed, unsigned long long step,
+                                               const Dims& D, const double r[3],
+                                               const double nd[3], bool tumble, bool rotate,
+                                               const float v[3], const float vm[3],
+                                               unsigned* status) {
   const float mP = (float)(c.mobility * c.P);
   for (int d = 0; d < 3; ++d) {
-    float rDot = mP * n0[d];
+    float rDot = mP * (float)nd[d];
     if (!c.translational_advection_off) rDot += v[d];
     swv[nsw * d + i] = f2d_exact(rDot);
     const double rn = advance_position(r[d], rDot, D.n[d]);
@@ -1122,12 +1160,81 @@ __device__ __forceinline__ void swimmers_move_block(
   }
 }
 
+// The rear point r - l n of a swimmer, as the dipole-end records compute it.
+__device__ __forceinline__ void rear_point(const double r[3], const double nd[3], double l,
+                                           double out[3]) {
+  for (int d = 0; d < 3; ++d) out[d] = __dsub_rn(r[d], __dmul_rn(nd[d], l));
+}
+
+template <class I = int>
+__device__ __forceinline__ void swimmers_move_block(
+    int blk, int nsw, double* __restrict__ swr, double* __restrict__ swv,
+    double* __restrict__ swn, lbswim_common_params c, unsigned long long seed,
+    unsigned long long step, Dims D, const float4* __restrict__ h, unsigned* status) {
+  constexpr int B = SWIMMERS_PER_BLOCK;
+  // stencils [0, B) at the swimmers, [B, 2B) at their rear points r - l n
+  __shared__ StencilSet<2 * B> st;
+  __shared__ float3 vel[2 * B];
+  const int t = threadIdx.x, i = blk * B + t;
+  const bool mine = t < B, valid = mine && i < nsw;
+  double r[3] = {0.0, 0.0, 0.0}, nd[3] = {0.0, 0.0, 0.0};
+  bool tumble = false, rotate = false;
+  if (valid) {
+    double rMinus[3];
+    for (int d = 0; d < 3; ++d) {
+      r[d] = swr[nsw * d + i];
+      nd[d] = swn[nsw * d + i];
+    }
+    tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
+    rotate = !tumble && !c.rotational_advection_off;
+    point_stencil(D, r, st, t);
+    if (rotate) {
+      rear_point(r, nd, c.l, rMinus);
+      point_stencil(D, rMinus, st, B + t);
+    } else {
+      st.active[B + t] = 0;
+    }
+  } else if (mine) {
+    st.active[t] = 0;
+    st.active[B + t] = 0;
+  }
+  __syncthreads();
+  gather_block_fixed<SWIMMER_LANES, 2 * SWIMMERS_PER_BLOCK, I>(h, D, st, vel);
+  __syncthreads();
+  if (!valid) return;
+  const float3 w = vel[t], wm = vel[B + t];
+  const float v[3] = {w.x, w.y, w.z}, vm[3] = {wm.x, wm.y, wm.z};
+  swimmer_update(i, nsw, swr, swv, swn, c, seed, step, D, r, nd, tumble, rotate, v, vm, status);
+}
+
 template <class I>
 __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
     lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
     const float4* __restrict__ h, unsigned* status) {
   swimmers_move_block<I>(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h, status);
+}
+
+// The same move from the velocities the step kernel interpolated at the
+// swimmers' dipole ends while it produced u (end 2i + 1 is the front point r,
+// end 2i the rear point): no gather from the velocity field.
+__global__ void __launch_bounds__(256) k_swimmers_move_gathered(
+    int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
+    lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
+    const unsigned long long* __restrict__ endvel, unsigned* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsw) return;
+  double r[3], nd[3];
+  float v[3], vm[3];
+  for (int d = 0; d < 3; ++d) {
+    r[d] = swr[nsw * d + i];
+    nd[d] = swn[nsw * d + i];
+    v[d] = vel_value((long long)endvel[3ll * (2 * i + 1) + d]);
+    vm[d] = vel_value((long long)endvel[3ll * (2 * i) + d]);
+  }
+  const bool tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
+  const bool rotate = !tumble && !c.rotational_advection_off;
+  swimmer_update(i, nsw, swr, swv, swn, c, seed, step, D, r, nd, tumble, rotate, v, vm, status);
 }
 
 // ---- batched ensembles: per-step reset, end records, moves --------------------
@@ -1280,6 +1387,11 @@ void spread_free(SpreadScratch& S) {
   S.bucket_list = nullptr;
   S.bucket_slabs = 0;
   S.bucket_tile = -1;
+  if (S.endvel) cudaFree(S.endvel);
+  S.endvel = nullptr;
+  S.endvel_capacity = 0;
+  S.gather_armed = SpreadScratch::GatherArm();
+  S.gathered = SpreadScratch::Gathered();
   free_lists(S.ftiles);
 }
 
@@ -1469,13 +1581,18 @@ static void append_ends_t(Swimmers* W, Lattice* L) {
     fill = S.bucket_tile == L->fused_tile;
   }
   if (S.pending == 0) LB_CUDA(cudaMemsetAsync(S.max_abs_force, 0, sizeof(unsigned), L->stream));
+  // zero the ends' velocity sums when the next step gathers them
+  const bool armed = BUCKETS && S.gather_armed.owner == W && S.pending == 0 && S.endvel &&
+                     S.endvel_capacity >= nends;
   if (nends > 0) {
     k_end_records<T><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
         W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L),
         (EndRecord<T>*)S.ends + S.pending, S.pending, S.max_abs_force, slab_grid(L),
-        fill ? S.bucket_count : nullptr, fill ? S.bucket_list : nullptr);
+        fill ? S.bucket_count : nullptr, fill ? S.bucket_list : nullptr,
+        armed ? S.endvel : nullptr);
     LB_CHECK_LAUNCH(1);
   }
+  if (!armed) S.gather_armed.owner = nullptr;
   S.pending += nends;
 }
 
@@ -1508,11 +1625,39 @@ void swimmers_add_forces(Swimmers* W, Lattice* L) {
   L->force_version++;
 }
 
+void spread_arm_gather(Swimmers* W, Lattice* L) {
+  SpreadScratch& S = L->spread;
+  S.gather_armed.owner = nullptr;
+  if (L->precision == LBSWIM_F64 || W->n <= 0) return;
+  const int nends = 2 * W->n;
+  if (S.endvel_capacity < nends) {
+    // earlier work on the stream may still use the old sums
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    if (S.endvel) cudaFree(S.endvel);
+    S.endvel = nullptr;
+    S.endvel_capacity = 0;
+    const int cap = std::max(nends + nends / 2, 64);
+    LB_CUDA(cudaMalloc(&S.endvel, sizeof(unsigned long long) * 3 * (size_t)cap));
+    S.endvel_capacity = cap;
+    S.prep.valid = false;  // its records zeroed the old sums
+  }
+  S.gather_armed.owner = W;
+  S.gather_armed.owner_step = W->step;
+  S.gather_armed.nends = nends;
+}
+
 void swimmers_move(Swimmers* W, Lattice* L) {
   const Dims D = make_dims(L);
+  SpreadScratch::Gathered& G = L->spread.gathered;
+  const bool gathered = G.valid && G.owner == W && G.owner_step == W->step &&
+                        L->precision != LBSWIM_F64;
+  G.valid = false;
   if (W->n > 0) {
     const int grid = (W->n + 255) / 256;
-    if (L->precision == LBSWIM_F64)
+    if (gathered)
+      k_swimmers_move_gathered<<<grid, 256, 0, L->stream>>>(
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, L->spread.endvel, L->status);
+    else if (L->precision == LBSWIM_F64)
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u,
           L->status);
@@ -1573,9 +1718,12 @@ void swimmers_move_preparing(Swimmers* W, Lattice* L, unsigned long long epoch) 
   }
   LB_CUDA(cudaMemsetAsync(P.bucket_count, 0, sizeof(unsigned) * nslabs, L->stream));
   LB_CUDA(cudaMemsetAsync(P.max_abs_force, 0, sizeof(unsigned), L->stream));
+  // the velocity sums of these ends start at zero for the step that spreads
+  // them (the move just above has read the previous ones)
+  unsigned long long* ev = L->spread.endvel_capacity >= nends ? L->spread.endvel : nullptr;
   k_end_records<float><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
       W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L), (EndRecord<float>*)P.ends, 0,
-      P.max_abs_force, G, P.bucket_count, P.bucket_list);
+      P.max_abs_force, G, P.bucket_count, P.bucket_list, ev);
   LB_CHECK_LAUNCH(1);
   if (!W->recorded) LB_CUDA(cudaEventCreateWithFlags(&W->recorded, cudaEventDisableTiming));
   LB_CUDA(cudaEventRecord(W->recorded, L->stream));
