@@ -392,8 +392,8 @@ def our_arm(args, world, rank, local):
     # step leaves idle.
     stream = torch.cuda.Stream(priority=-5)
     lat.set_stream(stream.cuda_stream)
-    if args.no_bulk_copy:
-        lat.set_compat(_lib.COMPAT_INIT_SXZ | _lib.COMPAT_NO_BULK_COPY)
+    if args.bulk_copy:
+        lat.set_compat(_lib.COMPAT_INIT_SXZ | _lib.COMPAT_BULK_COPY)
     upload(case, lat, sw, tr)
 
     def barrier():
@@ -500,25 +500,30 @@ def our_arm(args, world, rank, local):
     # the batched ensemble and the served stream, each against plain FP64
     # one solve at a time (every rank runs its own replica)
     if args.ens_members > 0:
-        line["ensemble"] = ensemble_arm(args)
+        line["ensemble"] = ensemble_arm(args, world, rank)
     if args.serve_seconds > 0:
-        line["serving"] = serving_arm(args)
+        line["serving"] = serving_arm(args, world, rank)
     emit(line, rank)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def ensemble_arm(args):
+def ensemble_arm(args, world=1, rank=0):
     """Batched ensemble of independent FP32 solves (shapes 16^3 .. 48x48x96,
     tau, swimmers and tracers drawn per solve) advanced together, against the
-    same solves stepped one at a time in plain FP64 (stepping timed only)."""
+    same solves stepped one at a time in plain FP64 (stepping timed only).
+    With several ranks the solves are shared out (lbswim.shard) and each rank
+    runs its share; rates are the job's total site updates over the slowest
+    rank's time."""
     import torch
-    from lbswim import serve
+    from lbswim import serve, shard
     from lbswim.ensemble import Ensemble
     from lbswim.System import System
     rng = np.random.default_rng(7)
-    specs = [serve.draw_spec(rng) for _ in range(args.ens_members)]
-    sites = sum(s.sites for s in specs)
+    all_specs = [serve.draw_spec(rng) for _ in range(args.ens_members)]
+    ranks = shard.assign(all_specs, world)
+    specs = [sp for _, sp in shard.mine(all_specs, ranks, rank)]
+    sites_all = sum(s.sites for s in all_specs)
     objs = [serve.build_solve(s, "f32") for s in specs]
     ens = Ensemble(objs)
     ens.autotune()
@@ -528,8 +533,8 @@ def ensemble_arm(args):
     t0 = time.perf_counter()
     ens.Step(args.ens_steps)
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    batched = sites * args.ens_steps / dt / 1e9
+    dt = max_over_ranks(time.perf_counter() - t0, world)
+    batched = sites_all * args.ens_steps / dt / 1e9
     del ens, objs
     # plain FP64, one solve at a time, the same solves
     f64_steps, f64_time = args.ens_f64_steps, 0.0
@@ -544,9 +549,10 @@ def ensemble_arm(args):
         system.Step(f64_steps)
         lat.synchronize()
         f64_time += time.perf_counter() - t0
-    plain = sites * f64_steps / f64_time / 1e9
+    f64_time = max_over_ranks(f64_time, world)
+    plain = sites_all * f64_steps / f64_time / 1e9
     # FP32 (batched) against FP64 velocity fields after the full run
-    chk = specs[:4]
+    chk = specs[:args.ens_check]
     cobjs = [serve.build_solve(sp, "f32") for sp in chk]
     cens = Ensemble(cobjs)
     cens.Step(args.ens_steps)
@@ -562,35 +568,62 @@ def ensemble_arm(args):
         lat32.u.D2H()
         a, b = lat32.u.data.reshape(3, -1), lat.u.data.reshape(3, -1)
         err = max(err, float(np.linalg.norm(a - b) / np.linalg.norm(b)))
-    return {"members": len(specs), "sites": sites, "steps": args.ens_steps, "precision": "f32",
+    err = max_over_ranks(err, world)
+    return {"members": len(all_specs), "ranks": world, "sites": sites_all,
+            "steps": args.ens_steps, "precision": "f32",
             "batched_glups": batched, "batched_s": dt,
             "plain_f64_glups": plain, "plain_f64_steps_timed": f64_steps,
             "speedup_vs_plain_f64": batched / plain,
-            "u_rel_l2_vs_f64": err, "u_check_members": len(chk),
+            "u_rel_l2_vs_f64": err, "u_check_members": len(chk) * world,
             "tiles": {"8x32": tiles.count(0), "16x16": tiles.count(1)},
             "launches_per_step": 4, "graph": "two steps captured, replayed"}
 
 
-def serving_arm(args):
+def serving_arm(args, world=1, rank=0):
     """Poisson arrivals of solves (the ensemble distribution plus 96^3 and
     128^3, steps log-uniform in [100, 5000]) served by continuous batching
-    under an HBM budget, and the same trace served one solve at a time in
-    plain FP64, each for the same wall time (or the plain one for
-    --serve-plain-seconds)."""
+    under an HBM budget -- each finished solve's state (u, swimmers, tracers)
+    read back to the host inside its latency -- at the BASELINE rate and at a
+    lower rate where the queue stays short (service time), and the same
+    BASELINE-rate trace served one solve at a time in plain FP64.  With
+    several ranks each serves its share of every stream (lbswim.shard)."""
     import torch
-    from lbswim import serve
-    rng = np.random.default_rng(11)
-    trace = serve.poisson_trace(rng, args.serve_rate, args.serve_seconds)
+    from lbswim import serve, shard
     free, _ = torch.cuda.mem_get_info()
     budget = int(0.6 * free)
-    srv = serve.Server(budget, chunk=64)
-    batched = serve.summary(srv.run(trace, args.serve_seconds))
-    del srv
+    sink = lambda index, result: None  # noqa: E731 -- the client takes the result
+
+    def served(rate, seconds, plain=False):
+        trace = serve.poisson_trace(np.random.default_rng(11), rate, seconds)
+        ranks = shard.assign_stream(trace, world)
+        local = shard.mine(trace, ranks, rank)
+        sub = [x for _, x in local]
+        if plain:
+            res = serve.serve_one_at_a_time(sub, seconds, "f64", readback=sink)
+        else:
+            srv = serve.Server(budget, chunk=64, readback=sink)
+            res = srv.run(sub, seconds)
+            res.pop("kept")
+            del srv
+        glob = [i for i, _ in local]
+        for d in res["done"]:
+            d["index"] = glob[d["index"]]
+        merged = shard.merge_served(shard.gather_objects(res, world))
+        out = serve.summary(merged)
+        out["arrivals"] = len(trace)
+        return out
+
+    batched = served(args.serve_rate, args.serve_seconds)
+    low = served(args.serve_rate_low, args.serve_seconds) if args.serve_rate_low > 0 else None
     plain_s = args.serve_plain_seconds or args.serve_seconds
-    plain = serve.summary(serve.serve_one_at_a_time(trace, plain_s, "f64"))
+    plain = served(args.serve_rate, plain_s, plain=True)
     return {"rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
-            "plain_seconds": plain_s,
-            "arrivals": len(trace), "hbm_budget_gb": budget / 1e9, "batched_f32": batched,
+            "plain_seconds": plain_s, "ranks": world,
+            "arrivals": batched["arrivals"], "hbm_budget_gb": budget / 1e9,
+            "result_readback": "u, swimmer r/v/n and tracer r/s/v of every finished solve copied "
+                               "to the host inside its latency",
+            "batched_f32": batched,
+            "batched_f32_low_rate": dict(low, rate_per_s=args.serve_rate_low) if low else None,
             "plain_f64": plain,
             "glups_ratio": (batched["glups"] / plain["glups"]) if plain["glups"] else None}
 
@@ -604,8 +637,9 @@ def main():
     ap.add_argument("--precision", default="f32", choices=["f64", "f32", "bf16", "f16"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-bulk-copy", action="store_true",
-                    help="step kernel with per-thread loads only (comparison runs)")
+    ap.add_argument("--bulk-copy", action="store_true",
+                    help="step kernel with bulk-copied rows and the in-kernel swimmer "
+                         "velocity gather (LBSWIM_COMPAT_BULK_COPY; comparison runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="timed CPU work of the cpu_baseline leg")
     ap.add_argument("--f64-steps", type=int, default=20,
@@ -613,11 +647,15 @@ def main():
     ap.add_argument("--ens-members", type=int, default=512,
                     help="batched-ensemble members (0: skip the ensemble figures)")
     ap.add_argument("--ens-steps", type=int, default=1000)
+    ap.add_argument("--ens-check", type=int, default=8,
+                    help="members checked against FP64 after the full run")
     ap.add_argument("--ens-f64-steps", type=int, default=20,
                     help="steps per solve timed for the plain FP64 rate")
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="wall time of each served stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-rate-low", type=float, default=50.0,
+                    help="a second, lower arrival rate for service-time latencies (0: skip)")
     ap.add_argument("--serve-plain-seconds", type=float, default=0.0,
                     help="wall time of the plain FP64 stream (0: as --serve-seconds)")
     args = ap.parse_args()

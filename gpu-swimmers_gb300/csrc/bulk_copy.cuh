@@ -48,14 +48,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// One bounded wait for the phase: the thread is suspended (not spinning) until
+// the phase completes or about MBAR_SUSPEND_NS pass.
+constexpr uint32_t MBAR_SUSPEND_NS = 100000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(done)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(MBAR_SUSPEND_NS)
       : "memory");
   return done != 0;
 }
@@ -74,13 +77,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* err,
                                           unsigned code) {
   if (mbar_try_wait(bar, parity)) return true;
+  // try_wait suspends the thread for a while in hardware; the timer and the
+  // status word are looked at only every 64 tries
   const unsigned long long t0 = global_ns();
-  for (;;) {
+  for (unsigned i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (err && (*(volatile unsigned*)err & code)) return false;
-    if (global_ns() - t0 > MBAR_WAIT_NS) {
-      if (err) atomicOr(err, code);
-      return false;
+    if ((i & 63) == 0) {
+      if (err && (*(volatile unsigned*)err & code)) return false;
+      if (global_ns() - t0 > MBAR_WAIT_NS) {
+        if (err) atomicOr(err, code);
+        return false;
+      }
     }
   }
 }

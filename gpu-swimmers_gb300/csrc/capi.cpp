@@ -239,7 +239,7 @@ int lbswim_lattice_set_compat(lbswim_lattice* lat, int flags) {
   check_lattice(lat);
   REQUIRE((flags & ~(LBSWIM_COMPAT_INIT_SXZ | LBSWIM_COMPAT_SYNC_STEP |
                       LBSWIM_COMPAT_EXACT_F64 | LBSWIM_COMPAT_WIDE_INDEX |
-                      LBSWIM_COMPAT_EAGER_FIELDS | LBSWIM_COMPAT_NO_BULK_COPY)) == 0,
+                      LBSWIM_COMPAT_EAGER_FIELDS | LBSWIM_COMPAT_BULK_COPY)) == 0,
           "unknown compat flag");
   LAT(lat)->compat = flags;
   API_END

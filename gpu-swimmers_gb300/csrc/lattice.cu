@@ -596,7 +596,6 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       hydro_moments(g, R, jx, jy, jz);
       if (!finite_f(R + jx + jy + jz)) raise_status(a.status, LBSWIM_STATUS_NONFINITE);
       S* __restrict__ fn = (S*)a.f_new;
-#pragma unroll
       S* __restrict__ bo = fn + fidx<S, I>(0, s, N);
 #pragma unroll
       for (int p = 0; p < 15; ++p) Store<S>::st(bo + p * 32, stored_from_dev<S>(g[p], p));
@@ -1006,10 +1005,11 @@ static void launch_fused_i(Lattice* L, const FusedArgs& a) {
 // reduced-precision buffers hold 15 f_sites(n) values).
 inline bool fits_int_index(long long n) { return 15 * ((n + 31) & ~31ll) < (1ll << 31); }
 
-// Rows of whole 32-site blocks are bulk-copied when the cross-section is 32
-// sites wide and nz a multiple of 32 (each row of the slab is then one block).
+// Rows of whole 32-site blocks are bulk-copied (LBSWIM_COMPAT_BULK_COPY) when
+// the cross-section is 32 sites wide and nz a multiple of 32 (each row of the
+// slab is then one block).
 inline bool fused_uses_tma(const Lattice* L, int TZ) {
-  return TZ == 32 && (L->size[2] & 31) == 0 && !(L->compat & LBSWIM_COMPAT_NO_BULK_COPY);
+  return TZ == 32 && (L->size[2] & 31) == 0 && (L->compat & LBSWIM_COMPAT_BULK_COPY);
 }
 
 // Whether a step with pending ends can also gather their velocities (the

@@ -1047,21 +1047,25 @@ __device__ __forceinline__ void gather_point_fixed(const float4* __restrict__ h,
   }
 }
 
+// Two points per group at a time (their loads in flight together), as
+// gather_block; NP * L is a multiple of 2 * blockDim.
 template <int L, int NP, class I = int>
 __device__ __forceinline__ void gather_block_fixed(const float4* __restrict__ h, const Dims& D,
                                                    const StencilSet<NP>& st, float3* vel) {
   const int sub = threadIdx.x & (L - 1);
   const int groups = blockDim.x / L;
-  for (int p = threadIdx.x / L; p < NP; p += groups) {
-    long long ax, ay, az;
-    gather_point_fixed<L, NP, I>(h, D, st, p, sub, ax, ay, az);
+  for (int p = threadIdx.x / L; p < NP; p += 2 * groups) {
+    long long a[6];
+    gather_point_fixed<L, NP, I>(h, D, st, p, sub, a[0], a[1], a[2]);
+    gather_point_fixed<L, NP, I>(h, D, st, p + groups, sub, a[3], a[4], a[5]);
 #pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1) {
-      ax += __shfl_xor_sync(0xffffffffu, ax, off);
-      ay += __shfl_xor_sync(0xffffffffu, ay, off);
-      az += __shfl_xor_sync(0xffffffffu, az, off);
+    for (int off = L / 2; off > 0; off >>= 1)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) a[c] += __shfl_xor_sync(0xffffffffu, a[c], off);
+    if (sub == 0) {
+      vel[p] = make_float3(vel_value(a[0]), vel_value(a[1]), vel_value(a[2]));
+      vel[p + groups] = make_float3(vel_value(a[3]), vel_value(a[4]), vel_value(a[5]));
     }
-    if (sub == 0) vel[p] = make_float3(vel_value(ax), vel_value(ay), vel_value(az));
   }
 }
 

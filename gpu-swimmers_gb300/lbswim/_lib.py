@@ -23,7 +23,7 @@ FIELD_COMPONENTS = {FIELD_RHO: 1, FIELD_U: 3, FIELD_FORCE: 3, FIELD_FOLD: 15, FI
 SW_R, SW_V, SW_N = 0, 1, 2
 TR_R, TR_S, TR_V = 0, 1, 2
 COMPAT_INIT_SXZ, COMPAT_SYNC_STEP, COMPAT_EXACT_F64, COMPAT_WIDE_INDEX = 1, 2, 4, 8
-COMPAT_EAGER_FIELDS, COMPAT_NO_BULK_COPY = 16, 32
+COMPAT_EAGER_FIELDS, COMPAT_BULK_COPY = 16, 32
 STATUS_NONFINITE, STATUS_PARTICLE_OUTSIDE, STATUS_COPY_TIMEOUT = 1, 2, 4
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",

@@ -90,10 +90,16 @@ extern "C" {
  * or a user's, may then read or add to LatticeData's device arrays).  The C++
  * class API of include/liblbswim/ sets it. */
 #define LBSWIM_COMPAT_EAGER_FIELDS 16
-/* FP32/BF16/FP16 lattices: the step kernel loads every site's distributions
- * with per-thread loads instead of bulk-copying whole rows into shared memory
- * (which it does when nz is a multiple of 32); the results are the same bits. */
-#define LBSWIM_COMPAT_NO_BULK_COPY 32
+/* FP32/BF16/FP16 lattices with nz a multiple of 32 and the 8 x 32 slab shape:
+ * the step kernel bulk-copies whole rows of distributions into shared memory
+ * (cp.async.bulk, completed on an mbarrier) instead of loading them thread by
+ * thread, and an FP32 lattice stepped by lbswim_system_step with one swimmer
+ * array also interpolates u(t+1) at the swimmers' dipole ends in the step
+ * kernel, which the swimmer move then takes.  The results are the same bits.
+ * Off by default: on GB300 the two-stage copy pipeline that fits beside the
+ * spreading state (two CTAs per SM) keeps too few bytes in flight, and the
+ * step ran slower (0.81 ms against 0.55 ms at 256^3, 1.05 ms with the gather). */
+#define LBSWIM_COMPAT_BULK_COPY 32
 
 /* ---- sticky status bits (lbswim_lattice_get_status) ----------------------- */
 /* No reference counterpart (the reference checks no kernel).  Kernels of a

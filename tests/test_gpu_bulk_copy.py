@@ -1,9 +1,12 @@
-"""The step kernel's bulk-copied rows (cp.async.bulk into shared memory, used
-when nz is a multiple of 32) give the same bits as its per-thread loads.
+"""The step kernel's bulk-copied rows (cp.async.bulk into shared memory, with
+LBSWIM_COMPAT_BULK_COPY when nz is a multiple of 32) give the same bits as its
+per-thread loads, and its interpolation of u(t+1) at the swimmers' dipole ends
+(the system step of an FP32 lattice with that flag) the same bits as the
+swimmer move's own gather from the velocity field.
 
-Same workload twice, one lattice with LBSWIM_COMPAT_NO_BULK_COPY: after system
-steps with pending forces, steps from a materialised dense force, and ragged
-slabs in x and y, every field and particle array is equal bit for bit.
+Same workload twice, one lattice with the flag: after system steps with
+pending forces, steps from a materialised dense force, and ragged slabs in x
+and y, every field and particle array is equal bit for bit.
 """
 import numpy as np
 import pytest
@@ -16,8 +19,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _pair(case, precision):
-    a = build_gpu(case, precision)
-    b = build_gpu(case, precision, compat=_lib.COMPAT_INIT_SXZ | _lib.COMPAT_NO_BULK_COPY)
+    a = build_gpu(case, precision, compat=_lib.COMPAT_INIT_SXZ | _lib.COMPAT_BULK_COPY)
+    b = build_gpu(case, precision)
     return a, b
 
 

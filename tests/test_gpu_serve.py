@@ -24,7 +24,7 @@ def test_solves_in_the_mix_equal_alone():
         trace.append((t, spec))
         t += 0.002
     budget = sum(s.device_bytes() for _, s in trace[:4])  # two must wait for memory
-    srv = serve.Server(budget, chunk=16, autotune=False)
+    srv = serve.Server(budget, chunk=16, autotune=False, readback=True)
     res = srv.run(trace, duration=60.0, drain=True, keep=set(range(len(trace))))
     assert len(res["done"]) == len(trace) and res["unfinished"] == 0
     assert max(d["queue"] for d in res["done"]) > 0.0  # someone waited for memory
@@ -40,6 +40,12 @@ def test_solves_in_the_mix_equal_alone():
         a, b = snapshot(*mixed), snapshot(lat, sw, tr)
         for k in a:
             assert np.array_equal(a[k], b[k]), (i, k)
+        # the result the server handed back is that state
+        got = next(d["result"] for d in res["done"] if d["index"] == i)
+        assert np.array_equal(got["u"].reshape(3, -1), b["u"]) and got["time_step"] == spec.steps
+        assert np.array_equal(got["sw_r"], b["sw_r"]) and np.array_equal(got["sw_n"], b["sw_n"])
+        if tr is not None:
+            assert np.array_equal(got["tr_r"], b["tr_r"])
 
 
 def test_summary_reports_latency_percentiles():

@@ -2,6 +2,7 @@
 distribution of the batched ensemble, the Poisson arrival stream and the
 latency summary of lbswim.serve."""
 import math
+import time
 
 import numpy as np
 
@@ -63,3 +64,96 @@ def test_device_bytes_grow_with_size_and_storage():
     assert b64 > b32 > b16
     # the distributions dominate: two f buffers of 15 values per site
     assert b32 > 2 * 15 * 4 * large.sites
+
+
+# ---- the serving loop's fault handling, with a fake GPU ----------------------
+class _FakeEnsemble:
+    """Stands in for the batched stepper: records memberships and steps, each
+    Step call taking `delay` seconds."""
+
+    def __init__(self, delay=0.0):
+        self.members, self.steps, self.delay = [], 0, delay
+
+    def set_members(self, members):
+        self.members = list(members)
+
+    def autotune(self):
+        pass
+
+    def Step(self, k):
+        assert self.members
+        self.steps += k
+        if self.delay:
+            time.sleep(self.delay)
+
+
+class _FakeBuild:
+    """Stands in for build_solve; `fail` maps a request seed to the number of
+    allocation failures (LBSWIM_ENOMEM) its first builds raise."""
+
+    def __init__(self, fail=None):
+        self.fail = dict(fail or {})
+        self.calls = 0
+
+    def __call__(self, spec, precision, lattice=None):
+        from lbswim import _lib
+        self.calls += 1
+        if self.fail.get(spec.seed, 0) > 0:
+            self.fail[spec.seed] -= 1
+            raise _lib.LbswimError(-3, "cudaMalloc: out of memory (injected)")
+        return (lattice or ("lattice", spec.seed), None, None)
+
+
+def _trace(n, steps=40, shape=(16, 16, 16)):
+    return [(0.0, serve.Spec(shape, 0.8, 4, 1e-3, 0.01, 8, 100 + i, steps)) for i in range(n)]
+
+
+def _outcomes(res, n):
+    seen = [d["index"] for d in res["done"]] + [r["index"] for r in res["rejected"]] + \
+        [c["index"] for c in res["cancelled"]]
+    assert sorted(seen) == list(range(n)), seen  # every request exactly once
+
+
+def test_malformed_and_oversized_requests_are_rejected_and_the_loop_goes_on():
+    trace = _trace(4)
+    trace[1] = (0.0, serve.Spec((16, 0, 16), 0.8, 4, 1e-3, 0.01, 8, 7, 40))       # bad shape
+    trace[2] = (0.0, serve.Spec((16, 16, 16), 0.8, 4, 1e-3, 0.01, 8, 8, 0))        # no steps
+    big = serve.Spec((512, 512, 512), 0.8, 4, 1e-3, 0.01, 8, 9, 40)
+    trace.append((0.0, big))
+    budget = 3 * trace[0][1].device_bytes()
+    srv = serve.Server(budget, chunk=16, build=_FakeBuild(), ensemble=_FakeEnsemble())
+    res = srv.run(trace, duration=5.0, drain=True)
+    _outcomes(res, len(trace))
+    why = {r["index"]: r["reason"] for r in res["rejected"]}
+    assert set(why) == {1, 2, 4}
+    assert "shape" in why[1] and "step" in why[2] and "budget" in why[4]
+    assert sorted(d["index"] for d in res["done"]) == [0, 3]
+
+
+def test_allocation_failures_wait_for_memory_or_reject():
+    trace = _trace(3)
+    budget = 3 * trace[0][1].device_bytes()
+    # request 1 fails twice while request 0 runs: it waits, then runs
+    build = _FakeBuild({trace[1][1].seed: 2})
+    srv = serve.Server(budget, chunk=8, build=build, ensemble=_FakeEnsemble())
+    res = srv.run(trace, duration=5.0, drain=True)
+    _outcomes(res, 3)
+    assert sorted(d["index"] for d in res["done"]) == [0, 1, 2] and not res["rejected"]
+    # alone, with nothing to free, a request whose allocation keeps failing is rejected
+    srv = serve.Server(budget, chunk=8, build=_FakeBuild({trace[0][1].seed: 99}),
+                       ensemble=_FakeEnsemble())
+    res = srv.run(trace[:1], duration=5.0, drain=True)
+    assert res["rejected"] == [{"index": 0, "reason": "device allocation failed"}]
+
+
+def test_cancelled_requests_leave_the_queue_and_the_batch():
+    trace = _trace(5, steps=4000)
+    trace[4] = (0.3, trace[4][1])  # arrives late
+    budget = 2 * trace[0][1].device_bytes()  # two run, the rest queue
+    srv = serve.Server(budget, chunk=64, build=_FakeBuild(), ensemble=_FakeEnsemble(0.002))
+    # 0 is running at 0.03 s (63 chunks of 2 ms each), 3 still queued
+    res = srv.run(trace, duration=10.0, drain=True, cancel={0: 0.03, 3: 0.03, 4: 0.1})
+    _outcomes(res, 5)
+    where = {c["index"]: c["where"] for c in res["cancelled"]}
+    assert where == {0: "batch", 3: "queue", 4: "before arrival"}
+    assert sorted(d["index"] for d in res["done"]) == [1, 2]
