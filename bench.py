@@ -638,8 +638,8 @@ def main():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bulk-copy", action="store_true",
-                    help="step kernel with bulk-copied rows and the in-kernel swimmer "
-                         "velocity gather (LBSWIM_COMPAT_BULK_COPY; comparison runs)")
+                    help="step kernel with bulk-copied rows (LBSWIM_COMPAT_BULK_COPY; "
+                         "comparison runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="timed CPU work of the cpu_baseline leg")
     ap.add_argument("--f64-steps", type=int, default=20,

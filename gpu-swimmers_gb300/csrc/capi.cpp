@@ -651,6 +651,14 @@ int lbswim_ensemble_step(lbswim_ensemble* ens, int nsteps) {
   API_END
 }
 
+int lbswim_ensemble_step_limited(lbswim_ensemble* ens, int nsteps, const int* limits) {
+  API_BEGIN
+  REQUIRE(ens, "ensemble handle is NULL");
+  REQUIRE(nsteps >= 0, "nsteps must be non-negative");
+  ensemble_step(reinterpret_cast<Ensemble*>(ens), nsteps, limits);
+  API_END
+}
+
 int lbswim_ensemble_autotune(lbswim_ensemble* ens) {
   API_BEGIN
   REQUIRE(ens, "ensemble handle is NULL");
@@ -711,13 +719,9 @@ int lbswim_system_step(lbswim_lattice* lat, lbswim_swimmers* const* swimmers, in
   const unsigned long long calls = g_calls.load(std::memory_order_relaxed);
   for (int t = 0; t < nsteps; ++t) {
     lattice_zero_force(L);  // ZeroForce
-    // with one swimmer array the step kernel also interpolates u(t+1) at the
-    // ends it spreads, and the move below takes those velocities
-    if (n_swimmers == 1) spread_arm_gather(SW(swimmers[0]), L);
     if (n_swimmers != 1 || !swimmers_add_forces_prepared(SW(swimmers[0]), L, calls))
       for (int i = 0; i < n_swimmers; ++i) swimmers_add_forces(SW(swimmers[i]), L);
     lattice_step(L);
-    L->spread.gather_armed.owner = nullptr;
     lattice_calc_hydro(L);
     // Tracers move on their own streams while the swimmers move and the next
     // step spreads forces; the step after that waits before overwriting the

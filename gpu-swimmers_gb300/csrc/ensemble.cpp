@@ -1,8 +1,8 @@
 // ensemble.cpp -- batched ensembles: many independent FP32 solves (each a
 // lattice with its swimmers and tracers) advanced together.
 //
-// One batched step is four launches over all members: a reset of the slab
-// counts, the dipole-end records of every swimmer array (listed under the
+// One batched step is five launches over all members: the step counter, a
+// reset of the slab counts, the dipole-end records of every swimmer array (listed under the
 // slabs they touch), one persistent step kernel that takes the slabs of every
 // member from a shared counter, and one move kernel over every swimmer and
 // tracer array.  Everything the kernels need comes from device tables, so the
@@ -202,13 +202,18 @@ static void build_tables(Ensemble* E) {
   }
 }
 
-void ensemble_step(Ensemble* E, int nsteps) {
+void ensemble_step(Ensemble* E, int nsteps, const int* limits) {
   const int n = (int)E->lat.size();
   if (n == 0 || nsteps <= 0) return;
   // every member's earlier work (its streams, tracer side streams) first
   LB_CUDA(cudaDeviceSynchronize());
   ensure_tables(E, n);
   build_tables(E);
+  std::vector<int> took(n);
+  for (int m = 0; m < n; ++m) {
+    took[m] = limits ? std::max(0, std::min(nsteps, limits[m])) : nsteps;
+    E->hmem[m].limit = took[m];
+  }
   LB_CUDA(cudaMemcpyAsync(E->t.nmem, &n, sizeof(int), cudaMemcpyHostToDevice, E->stream));
   LB_CUDA(cudaMemcpyAsync(E->t.mem, E->hmem.data(), sizeof(EnsMember) * n,
                           cudaMemcpyHostToDevice, E->stream));
@@ -223,16 +228,18 @@ void ensemble_step(Ensemble* E, int nsteps) {
   if (!E->g1) capture(E, 1, &E->g1);
   for (int i = 0; i < nsteps / 2; ++i) LB_CUDA(cudaGraphLaunch(E->g2, E->stream));
   if (nsteps & 1) LB_CUDA(cudaGraphLaunch(E->g1, E->stream));
-  count_launches(4ull * nsteps);
+  count_launches(5ull * nsteps);
   // the host copies above must outlive the copies: wait for the run
   LB_CUDA(cudaStreamSynchronize(E->stream));
   for (int m = 0; m < n; ++m) {
     Lattice* L = E->lat[m];
-    if (nsteps & 1) {
+    const int k = took[m];
+    if (k == 0) continue;
+    if (k & 1) {
       L->cur ^= 1;
       std::swap(L->hydro, L->hydro_shadow);
     }
-    L->time_step += nsteps;
+    L->time_step += k;
     L->f_version++;
     L->shadow_f_version = 0;  // rho, u of the last step are published
     L->force_version++;
@@ -240,8 +247,8 @@ void ensemble_step(Ensemble* E, int nsteps) {
     L->spread.pending = 2 * (E->sw[m] ? E->sw[m]->n : 0);
     L->spread.stepped = true;
     L->spread.bucket_tile = L->fused_tile;
-    if (E->sw[m]) E->sw[m]->step += nsteps;
-    if (E->tr[m]) E->tr[m]->moves_since_sort += nsteps;
+    if (E->sw[m]) E->sw[m]->step += k;
+    if (E->tr[m]) E->tr[m]->moves_since_sort += k;
   }
 }
 
@@ -294,6 +301,10 @@ static float time_shape(int nx, int ny, int nz, int tile, int copies) {
     }
     ensemble_set_members(E, L.data(), W.data(), nullptr, copies);
     ensemble_step(E, 2);  // warm-up, graphs
+    // the timed replays below run past that call's step count: no member limit
+    for (auto& M : E->hmem) M.limit = 1 << 30;
+    LB_CUDA(cudaMemcpyAsync(E->t.mem, E->hmem.data(), sizeof(EnsMember) * E->hmem.size(),
+                            cudaMemcpyHostToDevice, E->stream));
     LB_CUDA(cudaEventCreate(&e0));
     LB_CUDA(cudaEventCreate(&e1));
     LB_CUDA(cudaEventRecord(e0, E->stream));

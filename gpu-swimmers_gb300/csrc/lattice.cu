@@ -13,7 +13,6 @@
 
 #include <algorithm>
 #include <cstring>
-#include <type_traits>
 
 #include "bulk_copy.cuh"
 #include "lbswim_device.cuh"
@@ -356,11 +355,9 @@ constexpr int spread_base() {
   return align16(ring_pop_planes<true>() * (TY + 2) * (TZ + 2) * (int)sizeof(float));
 }
 
-// GATHER: the SPREAD instance also interpolates u(t+1) at the pending ends
-// (SlabSpreader::gather), for the swimmer move of the same coupled step.
-template <int TZ, int TY, bool SPREAD, bool GATHER = false>
+template <int TZ, int TY, bool SPREAD>
 constexpr int fused_smem_bytes() {
-  return SPREAD ? SpreadLayout<TZ, TY, 1, spread_base<TZ, TY>(), GATHER>::total
+  return SPREAD ? SpreadLayout<TZ, TY, 1, spread_base<TZ, TY>()>::total
                 : ring_pop_planes<false>() * (TY + 2) * (TZ + 2) * (int)sizeof(float);
 }
 
@@ -376,22 +373,20 @@ template <class S, int TY>
 constexpr int tma_row_bytes() { return 15 * 32 * (int)sizeof(S); }
 template <class S, int TY>
 constexpr int tma_stage_bytes() { return (TY + 2) * tma_row_bytes<S, TY>(); }
-template <class S, int TZ, int TY, bool SPREAD, bool GATHER>
-constexpr int tma_stage_offset() {
-  return (fused_smem_bytes<TZ, TY, SPREAD, GATHER>() + 127) & ~127;
-}
-template <class S, int TZ, int TY, bool SPREAD, bool GATHER>
+template <class S, int TZ, int TY, bool SPREAD>
+constexpr int tma_stage_offset() { return (fused_smem_bytes<TZ, TY, SPREAD>() + 127) & ~127; }
+template <class S, int TZ, int TY, bool SPREAD>
 constexpr int tma_bar_offset() {
-  return tma_stage_offset<S, TZ, TY, SPREAD, GATHER>() + TMA_STAGES * tma_stage_bytes<S, TY>();
+  return tma_stage_offset<S, TZ, TY, SPREAD>() + TMA_STAGES * tma_stage_bytes<S, TY>();
 }
-template <class S, int TZ, int TY, bool SPREAD, bool TMA, bool GATHER>
+template <class S, int TZ, int TY, bool SPREAD, bool TMA>
 constexpr int fused_smem_total() {
-  return TMA ? tma_bar_offset<S, TZ, TY, SPREAD, GATHER>() + 8 * TMA_STAGES
-             : fused_smem_bytes<TZ, TY, SPREAD, GATHER>();
+  return TMA ? tma_bar_offset<S, TZ, TY, SPREAD>() + 8 * TMA_STAGES
+             : fused_smem_bytes<TZ, TY, SPREAD>();
 }
 // two CTAs of the bulk-copy instances fit an SM's 228 KB (1 KB reserved each)
-static_assert(2 * (fused_smem_total<float, 32, 8, true, true, true>() + 1024) <= 228 * 1024,
-              "gathering bulk-copy slab smem");
+static_assert(2 * (fused_smem_total<float, 32, 8, true, true>() + 1024) <= 228 * 1024,
+              "bulk-copy slab smem");
 // two CTAs per SM (1 KB of each CTA's shared memory is reserved) within 132 KB
 static_assert(2 * (fused_smem_bytes<32, 8, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
 static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPREAD slab smem");
@@ -403,12 +398,10 @@ static_assert(2 * (fused_smem_bytes<16, 16, true>() + 1024) <= 132 * 1024, "SPRE
 // SPLIT: the form of the slab's force sums (slab_sums_split); SPREAD only.
 // TMA: the distributions of the cross-section's rows arrive by bulk copies
 // into shared memory (tma_* above); the lattice has nz a multiple of 32.
-template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT, bool TMA = false,
-          bool GATHER = false>
+template <class S, int TZ, int TY, bool SPREAD, class I, bool SPLIT, bool TMA = false>
 __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, int tx, int slab) {
   static_assert(sizeof(S) < 8, "the fused step serves the reduced-precision layouts");
   static_assert(!TMA || TZ == 32, "bulk-copied rows are whole 32-site blocks");
-  static_assert(!GATHER || SPREAD, "the gather uses the spreading's end lists");
   constexpr int NI = TY * TZ;
   constexpr int HZ = TZ + 2, HY = TY + 2, PLANE = HY * HZ;
   constexpr int NA = ring_slots<SPREAD>(0), NB = ring_slots<SPREAD>(1);
@@ -452,11 +445,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   const int my = ly * HZ + lz;
   // TMA: this thread's site is in a bulk-copied row (all but the z halo)
   const bool staged = TMA && active && lz >= 1 && lz <= ez;
-  S* stage = TMA ? reinterpret_cast<S*>(smraw + tma_stage_offset<S, TZ, TY, SPREAD, GATHER>())
-                 : nullptr;
+  S* stage = TMA ? reinterpret_cast<S*>(smraw + tma_stage_offset<S, TZ, TY, SPREAD>()) : nullptr;
   uint64_t* bars =
-      TMA ? reinterpret_cast<uint64_t*>(smraw + tma_bar_offset<S, TZ, TY, SPREAD, GATHER>())
-          : nullptr;
+      TMA ? reinterpret_cast<uint64_t*>(smraw + tma_bar_offset<S, TZ, TY, SPREAD>()) : nullptr;
   const int nrows = ey + 2;
   // Thread 0 arms the stage's barrier and copies the rows of local plane k
   // (x = x0 - 1 + k) into it.
@@ -488,7 +479,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   }
 
   // ---- this slab's pending dipole ends and the fixed-point force plane ----
-  SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>(), SPLIT, GATHER> sp;
+  SlabSpreader<TZ, TY, 1, spread_base<TZ, TY>(), SPLIT> sp;
   // the ring threads, which write no output plane, take the first pairs
   const int rt = tid >= NI ? tid - NI : tid + (int)blockDim.x - NI;
   if (SPREAD) {
@@ -525,9 +516,6 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
 #pragma unroll
     for (int i = 0; i < 18; ++i) cur[i] = pre[i];
     if (active && k + 1 < ex + 2) load(wrap_once(x0 + k, nx));
-    // u of output plane x0 + k - 3 (local plane k - 2), complete since the
-    // last barrier, at the pending ends
-    if (GATHER && k >= 3) sp.gather(k - 2, tid, blockDim.x);
     if constexpr (TMA) {
       // this plane's rows have landed in stage k % 2
       const int st = k & (TMA_STAGES - 1);
@@ -600,10 +588,8 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
 #pragma unroll
       for (int p = 0; p < 15; ++p) Store<S>::st(bo + p * 32, stored_from_dev<S>(g[p], p));
       const float inv = 1.0f / (a.rho0 + R);
-      const float4 hu = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
-                                    (jz + 0.5f * Fp2) * inv, R);
-      a.hydro[s] = hu;
-      if (GATHER) sp.put_u(ly, lz, hu.x, hu.y, hu.z);
+      a.hydro[s] = make_float4((jx + 0.5f * Fp0) * inv, (jy + 0.5f * Fp1) * inv,
+                               (jz + 0.5f * Fp2) * inv, R);
     }
     // the next plane's collision overwrites the slots just read, and the
     // scatter must be complete before the owners read it
@@ -616,22 +602,15 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
     keep1a = new1;
     k3 = k3 == 2 ? 0 : k3 + 1;
   }
-  if constexpr (GATHER) {
-    sp.gather(ex, tid, blockDim.x);  // the last output plane
-    __syncthreads();
-    sp.flush(tid, blockDim.x);
-  }
 }
 
-template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA, bool GATHER>
+template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA>
 __global__ void __launch_bounds__(TY * TZ + FUSED_RING_THREADS, 2) k_fused_step(FusedArgs a) {
   const int slab = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (!SPREAD || slab_sums_split(a.spread, slab, a.nx, a.ny, a.nz))
-    fused_slab<S, TZ, TY, SPREAD, I, true, TMA, GATHER>(a, blockIdx.x, blockIdx.y, blockIdx.z,
-                                                        slab);
+    fused_slab<S, TZ, TY, SPREAD, I, true, TMA>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
   else
-    fused_slab<S, TZ, TY, SPREAD, I, false, TMA, GATHER>(a, blockIdx.x, blockIdx.y, blockIdx.z,
-                                                         slab);
+    fused_slab<S, TZ, TY, SPREAD, I, false, TMA>(a, blockIdx.x, blockIdx.y, blockIdx.z, slab);
 }
 
 // ---------------------------------------------------------------------------
@@ -670,6 +649,10 @@ __global__ void __launch_bounds__(8 * 32 + FUSED_RING_THREADS, 2) k_ens_step(Ens
     if (tile >= total) break;
     const int m = ens_member_of(t.tile_prefix, nmem, tile);
     const EnsMember& M = t.mem[m];
+    if (*t.g_step >= M.limit) {  // the member has taken its steps of this run
+      __syncthreads();
+      continue;
+    }
     const int lt = tile - t.tile_prefix[m];
     const int tz = lt % M.nt[2], ty = (lt / M.nt[2]) % M.nt[1], tx = lt / (M.nt[2] * M.nt[1]);
     FusedArgs a{};
@@ -980,23 +963,23 @@ void lattice_init_from_hydro(Lattice* L) {
   L->f_version++;
 }
 
-template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA, bool GATHER = false>
+template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA>
 static void launch_fused_i(Lattice* L, const FusedArgs& a) {
-  constexpr int smem = fused_smem_total<S, TZ, TY, SPREAD, TMA, GATHER>();
+  constexpr int smem = fused_smem_total<S, TZ, TY, SPREAD, TMA>();
   static bool configured = false;  // per template instance, per process
   if (!configured) {
-    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA, GATHER>,
+    LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     // the bulk-copied rows bypass L1: give shared memory the whole carveout so
     // that two CTAs fit an SM
     if (TMA)
-      LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA, GATHER>,
+      LB_CUDA(cudaFuncSetAttribute(k_fused_step<S, TZ, TY, SPREAD, I, TMA>,
                                    cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared));
     configured = true;
   }
   dim3 grid((a.nz + TZ - 1) / TZ, (a.ny + TY - 1) / TY, (a.nx + FUSED_LX - 1) / FUSED_LX);
-  k_fused_step<S, TZ, TY, SPREAD, I, TMA, GATHER>
+  k_fused_step<S, TZ, TY, SPREAD, I, TMA>
       <<<grid, TY * TZ + FUSED_RING_THREADS, smem, L->stream>>>(a);
   LB_CHECK_LAUNCH(1);
 }
@@ -1012,23 +995,9 @@ inline bool fused_uses_tma(const Lattice* L, int TZ) {
   return TZ == 32 && (L->size[2] & 31) == 0 && (L->compat & LBSWIM_COMPAT_BULK_COPY);
 }
 
-// Whether a step with pending ends can also gather their velocities (the
-// bulk-copy instance of the 32 x 8 slab with 32-bit offsets, FP32 storage).
-template <class S>
-inline bool fused_can_gather(const Lattice* L) {
-  return std::is_same<S, float>::value && L->fused_tile == 0 && fused_uses_tma(L, 32) &&
-         fits_int_index(L->n) && !(L->compat & LBSWIM_COMPAT_WIDE_INDEX);
-}
-
 template <class S, int TZ, int TY, bool SPREAD>
 static void launch_fused(Lattice* L, const FusedArgs& a) {
   const bool wide = !fits_int_index(a.n) || (L->compat & LBSWIM_COMPAT_WIDE_INDEX);
-  if constexpr (SPREAD && TZ == 32 && std::is_same<S, float>::value) {
-    if (a.spread.endvel) {
-      launch_fused_i<S, TZ, TY, SPREAD, int, true, true>(L, a);
-      return;
-    }
-  }
   if constexpr (TZ == 32) {
     if (fused_uses_tma(L, TZ)) {
       if (wide)
@@ -1050,22 +1019,10 @@ constexpr bool STEP_SPREADS_IN_KERNEL = true;
 
 template <class S, int TZ, int TY>
 static void fused_step_tile(Lattice* L, FusedArgs& a) {
-  SpreadScratch& SS = L->spread;
-  SS.gathered.valid = false;
-  if (SS.pending > 0 && STEP_SPREADS_IN_KERNEL) {
+  if (L->spread.pending > 0 && STEP_SPREADS_IN_KERNEL) {
     const SlabSpread sp = spread_prepare_slabs(L);
-    // the swimmer move of this coupled step reads u(t+1) at the ends the step
-    // spreads: gather it here when the ends are those of one array and their
-    // velocity sums were zeroed with the records (lbswim_system_step)
-    const bool gather = SS.gather_armed.owner && SS.gather_armed.nends == sp.npending &&
-                        SS.endvel && fused_can_gather<S>(L);
     a.spread = SlabEnds{(const EndRecord<float>*)sp.ends, sp.count, sp.list, sp.npending,
-                        sp.max_abs_force, gather ? SS.endvel : nullptr};
-    if (gather) {
-      SS.gathered.valid = true;
-      SS.gathered.owner = SS.gather_armed.owner;
-      SS.gathered.owner_step = SS.gather_armed.owner_step;
-    }
+                        sp.max_abs_force};
     launch_fused<S, TZ, TY, true>(L, a);
   } else {
     launch_fused<S, TZ, TY, false>(L, a);
@@ -1199,8 +1156,6 @@ void lattice_calc_hydro(Lattice* L) {
     L->shadow_f_version = 0;
     return;
   }
-  // u is recomputed: velocities the step gathered at the ends may not be its
-  L->spread.gathered.valid = false;
   lattice_materialise_force(L);
   lattice_wait_readers(L, L->precision == LBSWIM_F64 ? nullptr : (const void*)L->hydro);
   switch (L->precision) {

@@ -572,21 +572,6 @@ __device__ __forceinline__ float node_contrib(float py, float pz, float wx, floa
   return (py * pz) * (wx * F);
 }
 
-// ---- fixed-point velocity interpolation (FP32 lattices) ------------------------
-// The interpolated velocity of a swimmer's dipole end (InterpVelocity,
-// interp.cu:8-47, at r and r - l n, SwimmerArray.cu:146,157) is a sum of 64
-// node contributions c = (phi_y phi_z)(phi_x u), each quantised to the 64-bit
-// integer round(c 2^VEL_FX_EXP) and summed exactly.  The sum does not depend on
-// the order or the grouping of its terms, so the step kernel, which adds them
-// plane by plane as it produces u, and the move kernel, which gathers them from
-// the stored field, give the same bits.  |c| < 2^13 (|u| < 2^14 in lattice
-// units) stays in range; the resolution 2^-44 is below FP32's for any c above
-// 2^-20, and contributions below 2^-13 (all of them while |u| < 1e-3) take the
-// one-conversion path of fx_quant.
-constexpr int VEL_FX_EXP = 44;
-__device__ __forceinline__ long long vel_quant(float c) { return fx_quant(c, 0x1.0p44f); }
-__device__ __forceinline__ float vel_value(long long q) { return fx_value(q, 0x1.0p-44f); }
-
 // Rank of key k among the cnt distinct keys: its position in increasing order.
 __device__ __forceinline__ int rank_of(int k, const int* keys, int cnt) {
   int r = 0;

@@ -101,23 +101,6 @@ struct SpreadScratch {
     int tile = -1;
     int nends = 0;
   } prep;
-  // Velocity sums of the pending ends ([capacity][3], fixed point, see
-  // vel_quant): lbswim_system_step with one swimmer array arms the gather
-  // (the records zero the sums), the next step kernel interpolates u(t+1) at
-  // the ends into them, and the swimmer move of the same coupled step reads
-  // them instead of gathering from the velocity field.
-  unsigned long long* endvel = nullptr;
-  int endvel_capacity = 0;
-  struct GatherArm {
-    const void* owner = nullptr;  // the Swimmers whose ends are pending
-    unsigned long long owner_step = 0;
-    int nends = 0;
-  } gather_armed;
-  struct Gathered {
-    bool valid = false;  // the last step kernel gathered, for this owner at this move step
-    const void* owner = nullptr;
-    unsigned long long owner_step = 0;
-  } gathered;
 };
 
 // What the fused step kernel needs to spread the pending ends itself.
@@ -244,6 +227,7 @@ struct EnsMember {
   double* tr_s;
   double* tr_v;
   unsigned* status;  // the member lattice's sticky status bits
+  int limit;         // steps this member takes in the current run (the run may take more)
 };
 
 // Device tables of an ensemble; the batched kernels of a captured step read
@@ -279,7 +263,9 @@ Ensemble* ensemble_new();
 void ensemble_delete(Ensemble* E);
 void ensemble_set_members(Ensemble* E, Lattice* const* lat, Swimmers* const* sw,
                           Tracers* const* tr, int n);
-void ensemble_step(Ensemble* E, int nsteps);
+// nsteps batched steps; member m takes only the first limits[m] of them when
+// limits is given (a member that finishes early leaves the batch).
+void ensemble_step(Ensemble* E, int nsteps, const int* limits = nullptr);
 void ensemble_autotune(Ensemble* E);
 int ensemble_size(const Ensemble* E);
 
@@ -329,9 +315,6 @@ void swimmers_move(Swimmers* S, Lattice* L);
 // last move prepared (false: nothing prepared that still holds), and the move
 // that prepares them for the next step.  epoch counts the API calls made.
 bool swimmers_add_forces_prepared(Swimmers* S, Lattice* L, unsigned long long epoch);
-// lbswim_system_step with one swimmer array on a reduced-precision lattice:
-// let the next step kernel gather the velocities of S's ends (before AddForces).
-void spread_arm_gather(Swimmers* S, Lattice* L);
 void swimmers_move_preparing(Swimmers* S, Lattice* L, unsigned long long epoch);
 // Wait on the host for the last kernel that used the swimmer arrays.
 void swimmers_wait(Swimmers* S);

@@ -328,7 +328,7 @@ __device__ __forceinline__ void end_records_block(
     int blk, int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P,
     double l, Dims D, EndRecord<T>* __restrict__ ends, int e_base,
     unsigned* __restrict__ max_abs_f, TileGrid G, unsigned* __restrict__ bucket_count,
-    int* __restrict__ bucket_list, unsigned long long* __restrict__ endvel = nullptr) {
+    int* __restrict__ bucket_list) {
   __shared__ EndRecord<T> srec[REC_THREADS];
   __shared__ unsigned smax;
   if (threadIdx.x == 0) smax = 0u;
@@ -370,9 +370,6 @@ __device__ __forceinline__ void end_records_block(
     }
     mbits = __float_as_uint(m);
     if (bucket_count) bucket_end(e_base + e, rec.o, D, G, bucket_count, bucket_list);
-    // the velocity sums the next step kernel adds to start at zero
-    if (endvel)
-      for (int c = 0; c < 3; ++c) endvel[3ll * (e_base + e) + c] = 0ull;
   }
   // non-negative floats order like their bit patterns: a warp's largest, then
   // one shared-memory atomic per warp
@@ -391,10 +388,9 @@ template <class T>
 __global__ void __launch_bounds__(REC_THREADS) k_end_records(
     int nsw, const double* __restrict__ r, const double* __restrict__ nv, double P, double l,
     Dims D, EndRecord<T>* __restrict__ ends, int e_base, unsigned* __restrict__ max_abs_f,
-    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list,
-    unsigned long long* __restrict__ endvel) {
+    TileGrid G, unsigned* __restrict__ bucket_count, int* __restrict__ bucket_list) {
   end_records_block<T>(blockIdx.x, nsw, r, nv, P, l, D, ends, e_base, max_abs_f, G, bucket_count,
-                       bucket_list, endvel);
+                       bucket_list);
 }
 
 // Slab buckets of recorded ends (the slab shape changed since they were recorded).
@@ -1003,72 +999,6 @@ __device__ __forceinline__ void gather_block(const float4* __restrict__ h, const
   }
 }
 
-// The swimmers' interpolation in fixed point (vel_quant): lane `sub` of the L
-// lanes of a point takes z node sub & 3 and y nodes sub >> 2, sub >> 2 + L/4,
-// ..., over the x planes of the stencil -- its four nodes, or for nx < 4 the
-// planes the nodes fold onto, with their summed weights (axis_weight), as the
-// step kernel's plane-by-plane gather sees them -- so that the sums equal the
-// step kernel's bit for bit.
-template <int L, int NP, class I = int>
-__device__ __forceinline__ void gather_point_fixed(const float4* __restrict__ h, const Dims& D,
-                                                   const StencilSet<NP>& s, int p, int sub,
-                                                   long long& ax, long long& ay, long long& az) {
-  ax = ay = az = 0;
-  if (!s.active[p]) return;
-  const int nx = D.n[0], nz = D.n[2];
-  const I nynz = (I)D.n[1] * nz;
-  const int kz = sub & 3;
-  const int z = node_after(s.o[2][p], kz, nz);
-  const float pz = s.w[2][kz][p];
-  const int np = nx >= 4 ? 4 : nx;
-  I xo[4];
-  float wx[4];
-  float phx[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) phx[i] = s.w[0][i][p];
-#pragma unroll
-  for (int ix = 0; ix < 4; ++ix) {
-    const int gx = nx >= 4 ? node_after(s.o[0][p], ix, nx) : ix;
-    xo[ix] = (I)gx * nynz;
-    wx[ix] = nx >= 4 ? phx[ix] : (ix < nx ? axis_weight(ix, s.o[0][p], nx, phx) : 0.f);
-  }
-#pragma unroll
-  for (int jy = sub >> 2; jy < 4; jy += L / 4) {
-    const I yz = (I)node_after(s.o[1][p], jy, D.n[1]) * nz + z;
-    const float py = s.w[1][jy][p];
-#pragma unroll
-    for (int ix = 0; ix < 4; ++ix) {
-      if (ix >= np) break;
-      const float4 q = __ldg(h + xo[ix] + yz);
-      ax += vel_quant(node_contrib(py, pz, wx[ix], q.x));
-      ay += vel_quant(node_contrib(py, pz, wx[ix], q.y));
-      az += vel_quant(node_contrib(py, pz, wx[ix], q.z));
-    }
-  }
-}
-
-// Two points per group at a time (their loads in flight together), as
-// gather_block; NP * L is a multiple of 2 * blockDim.
-template <int L, int NP, class I = int>
-__device__ __forceinline__ void gather_block_fixed(const float4* __restrict__ h, const Dims& D,
-                                                   const StencilSet<NP>& st, float3* vel) {
-  const int sub = threadIdx.x & (L - 1);
-  const int groups = blockDim.x / L;
-  for (int p = threadIdx.x / L; p < NP; p += 2 * groups) {
-    long long a[6];
-    gather_point_fixed<L, NP, I>(h, D, st, p, sub, a[0], a[1], a[2]);
-    gather_point_fixed<L, NP, I>(h, D, st, p + groups, sub, a[3], a[4], a[5]);
-#pragma unroll
-    for (int off = L / 2; off > 0; off >>= 1)
-#pragma unroll
-      for (int c = 0; c < 6; ++c) a[c] += __shfl_xor_sync(0xffffffffu, a[c], off);
-    if (sub == 0) {
-      vel[p] = make_float3(vel_value(a[0]), vel_value(a[1]), vel_value(a[2]));
-      vel[p + groups] = make_float3(vel_value(a[3]), vel_value(a[4]), vel_value(a[5]));
-    }
-  }
-}
-
 constexpr int TRACER_MOVE_BLOCK = 256;
 constexpr int TRACER_LANES = 4;  // lanes per interpolation point
 
@@ -1203,7 +1133,7 @@ __device__ __forceinline__ void swimmers_move_block(
     st.active[B + t] = 0;
   }
   __syncthreads();
-  gather_block_fixed<SWIMMER_LANES, 2 * SWIMMERS_PER_BLOCK, I>(h, D, st, vel);
+  gather_block<SWIMMER_LANES, 2 * SWIMMERS_PER_BLOCK, I>(h, D, st, vel);
   __syncthreads();
   if (!valid) return;
   const float3 w = vel[t], wm = vel[B + t];
@@ -1217,28 +1147,6 @@ __global__ void __launch_bounds__(SWIMMER_MOVE_BLOCK) k_swimmers_move_f32(
     lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
     const float4* __restrict__ h, unsigned* status) {
   swimmers_move_block<I>(blockIdx.x, nsw, swr, swv, swn, c, seed, step, D, h, status);
-}
-
-// The same move from the velocities the step kernel interpolated at the
-// swimmers' dipole ends while it produced u (end 2i + 1 is the front point r,
-// end 2i the rear point): no gather from the velocity field.
-__global__ void __launch_bounds__(256) k_swimmers_move_gathered(
-    int nsw, double* __restrict__ swr, double* __restrict__ swv, double* __restrict__ swn,
-    lbswim_common_params c, unsigned long long seed, unsigned long long step, Dims D,
-    const unsigned long long* __restrict__ endvel, unsigned* status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nsw) return;
-  double r[3], nd[3];
-  float v[3], vm[3];
-  for (int d = 0; d < 3; ++d) {
-    r[d] = swr[nsw * d + i];
-    nd[d] = swn[nsw * d + i];
-    v[d] = vel_value((long long)endvel[3ll * (2 * i + 1) + d]);
-    vm[d] = vel_value((long long)endvel[3ll * (2 * i) + d]);
-  }
-  const bool tumble = rng_uniform(seed, (uint32_t)i, step) < c.alpha;
-  const bool rotate = !tumble && !c.rotational_advection_off;
-  swimmer_update(i, nsw, swr, swv, swn, c, seed, step, D, r, nd, tumble, rotate, v, vm, status);
 }
 
 // ---- batched ensembles: per-step reset, end records, moves --------------------
@@ -1264,16 +1172,20 @@ __device__ __forceinline__ Dims ens_dims(const EnsMember& M) {
   return D;
 }
 
-// Zero every member's slab counts and largest |F|, the slab counter of this
-// parity, and advance the run's step counter.
+// Advance the run's step counter (its own launch, so that every block of the
+// step's kernels reads the same step index).
+__global__ void k_ens_tick(EnsTable t) { *t.g_step += 1; }
+
+// Zero the slab counts and largest |F| of every member still stepping, and
+// the slab counter of this parity.
+
 __global__ void k_ens_reset(EnsTable t, int parity) {
   const int nmem = *t.nmem;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    t.counters[parity] = 0u;
-    *t.g_step += 1;
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) t.counters[parity] = 0u;
+  const long long g = *t.g_step;
   for (int m = blockIdx.x; m < nmem; m += gridDim.x) {
     const EnsMember& M = t.mem[m];
+    if (g >= M.limit) continue;
     const int nslabs = M.nt[0] * M.nt[1] * M.nt[2];
     for (int i = threadIdx.x; i < nslabs; i += blockDim.x) M.bucket_count[i] = 0u;
     if (threadIdx.x == 0) *M.max_abs_f = 0u;
@@ -1286,6 +1198,7 @@ __global__ void __launch_bounds__(REC_THREADS) k_ens_records(EnsTable t) {
   for (int vb = blockIdx.x; vb < total; vb += gridDim.x) {
     const int m = ens_find(t.rec_prefix, nmem, vb);
     const EnsMember& M = t.mem[m];
+    if (*t.g_step >= M.limit) continue;
     TileGrid G;
     slab_shape_of_dev(M.tile, G.T);
     G.h = 1;
@@ -1310,11 +1223,13 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_ens_move(EnsTable t, int 
     if (vb < nsb) {
       const int m = ens_find(t.sw_prefix, nmem, vb);
       const EnsMember& M = t.mem[m];
+      if ((long long)g >= M.limit) continue;  // uniform in the block: no barrier skipped
       swimmers_move_block(vb - t.sw_prefix[m], M.nsw, M.sw_r, M.sw_v, M.sw_n, M.common, M.seed,
                           M.step0 + g, ens_dims(M), (const float4*)M.hyd[parity], M.status);
     } else {
       const int m = ens_find(t.tr_prefix, nmem, vb - nsb);
       const EnsMember& M = t.mem[m];
+      if ((long long)g >= M.limit) continue;
       tracers_move_block(vb - nsb - t.tr_prefix[m], M.ntr, M.tr_r, M.tr_s, M.tr_v, ens_dims(M),
                          (const float4*)M.hyd[parity], M.status);
     }
@@ -1323,8 +1238,9 @@ __global__ void __launch_bounds__(TRACER_MOVE_BLOCK) k_ens_move(EnsTable t, int 
 }
 
 void ens_launch_reset(const EnsTable& t, int parity, cudaStream_t s) {
+  k_ens_tick<<<1, 1, 0, s>>>(t);
   k_ens_reset<<<152, 256, 0, s>>>(t, parity);
-  LB_CHECK_LAUNCH(1);
+  LB_CHECK_LAUNCH(2);
 }
 void ens_launch_records(const EnsTable& t, int grid, cudaStream_t s) {
   k_ens_records<<<grid, REC_THREADS, 0, s>>>(t);
@@ -1391,11 +1307,6 @@ void spread_free(SpreadScratch& S) {
   S.bucket_list = nullptr;
   S.bucket_slabs = 0;
   S.bucket_tile = -1;
-  if (S.endvel) cudaFree(S.endvel);
-  S.endvel = nullptr;
-  S.endvel_capacity = 0;
-  S.gather_armed = SpreadScratch::GatherArm();
-  S.gathered = SpreadScratch::Gathered();
   free_lists(S.ftiles);
 }
 
@@ -1585,18 +1496,13 @@ static void append_ends_t(Swimmers* W, Lattice* L) {
     fill = S.bucket_tile == L->fused_tile;
   }
   if (S.pending == 0) LB_CUDA(cudaMemsetAsync(S.max_abs_force, 0, sizeof(unsigned), L->stream));
-  // zero the ends' velocity sums when the next step gathers them
-  const bool armed = BUCKETS && S.gather_armed.owner == W && S.pending == 0 && S.endvel &&
-                     S.endvel_capacity >= nends;
   if (nends > 0) {
     k_end_records<T><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
         W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L),
         (EndRecord<T>*)S.ends + S.pending, S.pending, S.max_abs_force, slab_grid(L),
-        fill ? S.bucket_count : nullptr, fill ? S.bucket_list : nullptr,
-        armed ? S.endvel : nullptr);
+        fill ? S.bucket_count : nullptr, fill ? S.bucket_list : nullptr);
     LB_CHECK_LAUNCH(1);
   }
-  if (!armed) S.gather_armed.owner = nullptr;
   S.pending += nends;
 }
 
@@ -1629,39 +1535,11 @@ void swimmers_add_forces(Swimmers* W, Lattice* L) {
   L->force_version++;
 }
 
-void spread_arm_gather(Swimmers* W, Lattice* L) {
-  SpreadScratch& S = L->spread;
-  S.gather_armed.owner = nullptr;
-  if (L->precision == LBSWIM_F64 || W->n <= 0) return;
-  const int nends = 2 * W->n;
-  if (S.endvel_capacity < nends) {
-    // earlier work on the stream may still use the old sums
-    LB_CUDA(cudaStreamSynchronize(L->stream));
-    if (S.endvel) cudaFree(S.endvel);
-    S.endvel = nullptr;
-    S.endvel_capacity = 0;
-    const int cap = std::max(nends + nends / 2, 64);
-    LB_CUDA(cudaMalloc(&S.endvel, sizeof(unsigned long long) * 3 * (size_t)cap));
-    S.endvel_capacity = cap;
-    S.prep.valid = false;  // its records zeroed the old sums
-  }
-  S.gather_armed.owner = W;
-  S.gather_armed.owner_step = W->step;
-  S.gather_armed.nends = nends;
-}
-
 void swimmers_move(Swimmers* W, Lattice* L) {
   const Dims D = make_dims(L);
-  SpreadScratch::Gathered& G = L->spread.gathered;
-  const bool gathered = G.valid && G.owner == W && G.owner_step == W->step &&
-                        L->precision != LBSWIM_F64;
-  G.valid = false;
   if (W->n > 0) {
     const int grid = (W->n + 255) / 256;
-    if (gathered)
-      k_swimmers_move_gathered<<<grid, 256, 0, L->stream>>>(
-          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, L->spread.endvel, L->status);
-    else if (L->precision == LBSWIM_F64)
+    if (L->precision == LBSWIM_F64)
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u,
           L->status);
@@ -1722,12 +1600,9 @@ void swimmers_move_preparing(Swimmers* W, Lattice* L, unsigned long long epoch) 
   }
   LB_CUDA(cudaMemsetAsync(P.bucket_count, 0, sizeof(unsigned) * nslabs, L->stream));
   LB_CUDA(cudaMemsetAsync(P.max_abs_force, 0, sizeof(unsigned), L->stream));
-  // the velocity sums of these ends start at zero for the step that spreads
-  // them (the move just above has read the previous ones)
-  unsigned long long* ev = L->spread.endvel_capacity >= nends ? L->spread.endvel : nullptr;
   k_end_records<float><<<(nends + REC_THREADS - 1) / REC_THREADS, REC_THREADS, 0, L->stream>>>(
       W->n, W->r, W->nv, W->common.P, W->common.l, make_dims(L), (EndRecord<float>*)P.ends, 0,
-      P.max_abs_force, G, P.bucket_count, P.bucket_list, ev);
+      P.max_abs_force, G, P.bucket_count, P.bucket_list);
   LB_CHECK_LAUNCH(1);
   if (!W->recorded) LB_CUDA(cudaEventCreateWithFlags(&W->recorded, cudaEventDisableTiming));
   LB_CUDA(cudaEventRecord(W->recorded, L->stream));

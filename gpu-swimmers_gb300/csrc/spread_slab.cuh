@@ -51,9 +51,7 @@ __device__ __forceinline__ int wrap_small(int i, int n) {
 // fixed-point sums of one plane [3][PLANE][2 words], coverage masks [CAP] (u64),
 // ends [CAP], local node rows [CAP], per-plane list offsets [LX + 2H + 1],
 // plane lists [CAP * SPREAD_PLANES_PER_END] (u16).
-// GATHER adds the velocity gather of the step kernel: per-end fixed-point
-// velocity sums [CAP][3] (long long) and the output plane's u [3][TY * TZ].
-template <int TZ, int TY, int H, int BASE, bool GATHER = false>
+template <int TZ, int TY, int H, int BASE>
 struct SpreadLayout {
   static constexpr int PLANE = (TY + 2 * H) * (TZ + 2 * H);
   static constexpr int fq = align16(BASE);
@@ -62,9 +60,7 @@ struct SpreadLayout {
   static constexpr int nodes = align16(ends + SPREAD_CAP * (int)sizeof(SlabEnd));
   static constexpr int poff = align16(nodes + SPREAD_CAP * (int)sizeof(NodeLocal));
   static constexpr int plist = align16(poff + (SLAB_LX + 2 * H + 1) * 4);
-  static constexpr int vacc = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END * 2);
-  static constexpr int uplane = align16(vacc + (GATHER ? SPREAD_CAP * 3 * 8 : 0));
-  static constexpr int total = align16(uplane + (GATHER ? 3 * TY * TZ * 4 : 0));
+  static constexpr int total = align16(plist + SPREAD_CAP * SPREAD_PLANES_PER_END * 2);
 };
 
 // Where the ends of slab `slab` are: its bucket, or every pending end when the
@@ -75,10 +71,6 @@ struct SlabEnds {
   const int* list;        // [slabs][SLAB_BUCKET_CAP]
   int npending;
   const unsigned* max_abs_f;
-  // [npending][3] fixed-point velocity sums of the ends (vel_quant), zero
-  // before the step; the step kernel adds u(t+1) interpolated at every end.
-  // Null: no gather.
-  unsigned long long* endvel;
 };
 
 // Whether the sums of slab `slab` can take the split form: a site takes at
@@ -96,15 +88,14 @@ __device__ __forceinline__ bool slab_sums_split(const SlabEnds& se, int slab, in
 // SPLIT: the sums are (sum of the low 16 bits, sum of q >> 16), each added
 // with an atomic that returns nothing; otherwise 64-bit sums whose high word
 // takes the low word's carries (slab_sums_split decides).
-template <int TZ, int TY, int H, int BASE, bool SPLIT, bool GATHER = false>
+template <int TZ, int TY, int H, int BASE, bool SPLIT>
 struct SlabSpreader {
   static constexpr int HZ = TZ + 2 * H, PLANE = (TY + 2 * H) * HZ;
-  using SL = SpreadLayout<TZ, TY, H, BASE, GATHER>;
+  using SL = SpreadLayout<TZ, TY, H, BASE>;
   unsigned char* smem;
   int nx, ny, nz, x0, y0, z0, ex, ey, ez;
   const EndRecord<float>* ends;
   const int* list;
-  unsigned long long* endvel;
   long long s0;
   int cnt;
   bool in_smem, overflow;
@@ -120,8 +111,6 @@ struct SlabSpreader {
   __device__ unsigned short* plist() const {
     return reinterpret_cast<unsigned short*>(smem + SL::plist);
   }
-  __device__ long long* vacc() const { return reinterpret_cast<long long*>(smem + SL::vacc); }
-  __device__ float* uplane() const { return reinterpret_cast<float*>(smem + SL::uplane); }
 
   __device__ void bind(unsigned char* smem_, const SlabEnds& se, int slab, int nx_, int ny_,
                        int nz_, int x0_, int y0_, int z0_, int ex_, int ey_, int ez_) {
@@ -132,7 +121,6 @@ struct SlabSpreader {
     fx_inv = exp2_int(-e);
     ends = se.ends;
     list = se.list;
-    endvel = GATHER ? se.endvel : nullptr;
     const unsigned c = se.count[slab];
     overflow = c > (unsigned)SLAB_BUCKET_CAP;
     cnt = overflow ? se.npending : (int)c;
@@ -180,8 +168,6 @@ struct SlabSpreader {
       }
     }
     for (int i = tid; i < 3 * 2 * PLANE; i += nthreads) fq()[i] = 0u;
-    if (GATHER && in_smem)
-      for (int i = tid; i < 3 * cnt; i += nthreads) vacc()[i] = 0ll;
     __syncthreads();
     if (in_smem) {
       // per-plane lists in increasing end position: count, offsets, fill
@@ -288,102 +274,6 @@ struct SlabSpreader {
           for (int lz2 = wrap_any(zg - z0 + H, nz); lz2 <= ez - 1 + 2 * H; lz2 += nz)
             add3(ly2 * HZ + lz2, q0, q1, q2);
       }
-    }
-  }
-
-  // ---- velocity gather (GATHER instances; H = 1, the step kernel) ----------
-  // u(t+1) of interior site (ly, lz), 1 <= ly <= ey, 1 <= lz <= ez, of the
-  // output plane, for gather().
-  __device__ void put_u(int ly, int lz, float ux, float uy, float uz) const {
-    float* u = uplane();
-    const int at = (ly - H) * TZ + (lz - H);
-    u[at] = ux;
-    u[TY * TZ + at] = uy;
-    u[2 * TY * TZ + at] = uz;
-  }
-
-  // Add u of output plane kk (put_u) interpolated at every end whose stencil
-  // has nodes in the interior of that plane: the nodes' contributions
-  // (phi_y phi_z)(phi_x u), quantised (vel_quant), into the end's sums.  A
-  // half-warp takes one (end, plane) entry, a lane one (jy, jz) node; the
-  // half-warp adds its 16 integers and one lane adds them to the end's sums
-  // (every end has at most one entry per plane).  The block's threads call it
-  // together, with nthreads a multiple of 16.
-  __device__ void gather(int kk, int tid, int nthreads) const {
-    const int gx = wrap_once(x0 - H + kk, nx);
-    const float* u = uplane();
-    if (in_smem) {
-      const int p0 = poff()[kk], np = poff()[kk + 1] - p0;
-      const unsigned hmask = 0xffffu << (tid & 16);
-      for (int t = tid; t < np * 16; t += nthreads) {
-        const unsigned ent = plist()[p0 + (t >> 4)];
-        const int q = (int)(ent & 0xffu);
-        const int jy = (t >> 2) & 3, jz = t & 3;
-        long long a0 = 0, a1 = 0, a2 = 0;
-        const int ly2 = nodes()[q].y[jy], lz2 = nodes()[q].z[jz];
-        if ((ly2 | lz2) >= 0) {
-          // the node's place in the interior; a node that appears twice in
-          // the cross-section (tiny lattices) is interior at one place at most
-          const int ly = ly2 >= H ? ly2 : ly2 + ny, lz = lz2 >= H ? lz2 : lz2 + nz;
-          if (ly <= ey - 1 + H && lz <= ez - 1 + H) {
-            const SlabEnd& e = srec()[q];
-            float wx;
-            if (ent & PL_FOLD)
-              cover_weight(gx, e.ox, nx, e.phi[0], wx);
-            else
-              wx = e.phi[0][(ent >> 8) & 3u];
-            const float py = e.phi[1][jy], pz = e.phi[2][jz];
-            const int at = (ly - H) * TZ + (lz - H);
-            a0 = vel_quant(node_contrib(py, pz, wx, u[at]));
-            a1 = vel_quant(node_contrib(py, pz, wx, u[TY * TZ + at]));
-            a2 = vel_quant(node_contrib(py, pz, wx, u[2 * TY * TZ + at]));
-          }
-        }
-#pragma unroll
-        for (int off = 8; off > 0; off >>= 1) {
-          a0 += __shfl_xor_sync(hmask, a0, off);
-          a1 += __shfl_xor_sync(hmask, a1, off);
-          a2 += __shfl_xor_sync(hmask, a2, off);
-        }
-        if ((t & 15) == 0 && (a0 | a1 | a2)) {
-          long long* v = vacc() + 3 * q;
-          v[0] += a0;
-          v[1] += a1;
-          v[2] += a2;
-        }
-      }
-    } else {
-      // more ends than shared memory holds: every contribution straight to
-      // the ends' sums in global memory
-      for (int t = tid; t < cnt * 16; t += nthreads) {
-        const int eid = overflow ? (t >> 4) : list[s0 + (t >> 4)];
-        const EndRecord<float>& e = ends[eid];
-        float wx;
-        if (!cover_weight(gx, e.o[0], nx, e.phi[0], wx)) continue;
-        const int jy = (t >> 2) & 3, jz = t & 3;
-        const float py = e.phi[1][jy], pz = e.phi[2][jz];
-        const int yg = wrap_any(e.o[1] + jy, ny), zg = wrap_any(e.o[2] + jz, nz);
-        int ly = wrap_any(yg - y0 + H, ny), lz = wrap_any(zg - z0 + H, nz);
-        if (ly < H) ly += ny;
-        if (lz < H) lz += nz;
-        if (ly > ey - 1 + H || lz > ez - 1 + H) continue;
-        const int at = (ly - H) * TZ + (lz - H);
-        const long long a[3] = {vel_quant(node_contrib(py, pz, wx, u[at])),
-                                vel_quant(node_contrib(py, pz, wx, u[TY * TZ + at])),
-                                vel_quant(node_contrib(py, pz, wx, u[2 * TY * TZ + at]))};
-        for (int c = 0; c < 3; ++c)
-          if (a[c]) atomicAdd(endvel + 3ll * eid + c, (unsigned long long)a[c]);
-      }
-    }
-  }
-
-  // The slab's velocity sums of its ends into the global ones (after the last
-  // gather and a barrier).
-  __device__ void flush(int tid, int nthreads) const {
-    if (!in_smem) return;
-    for (int i = tid; i < 3 * cnt; i += nthreads) {
-      const long long v = vacc()[i];
-      if (v) atomicAdd(endvel + 3ll * list[s0 + i / 3] + i % 3, (unsigned long long)v);
     }
   }
 

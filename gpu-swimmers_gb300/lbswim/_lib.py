@@ -94,6 +94,7 @@ _PROTOS = {
     "lbswim_ensemble_set_members": (C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP),
                                               C.POINTER(_VP), C.c_int]),
     "lbswim_ensemble_step": (C.c_int, [_VP, C.c_int]),
+    "lbswim_ensemble_step_limited": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int)]),
     "lbswim_ensemble_autotune": (C.c_int, [_VP]),
     "lbswim_lattice_device_ptr": (C.c_int, [_VP, C.c_int, C.POINTER(_VP), C.POINTER(C.c_int)]),
     "lbswim_lattice_set_timing": (C.c_int, [_VP, C.c_int]),

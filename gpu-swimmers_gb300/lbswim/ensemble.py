@@ -44,8 +44,16 @@ class Ensemble:
         _lib.check(_lib.lib.lbswim_ensemble_set_members(self._h, lat, sw, tr, n))
         self._members = members
 
-    def Step(self, nsteps=1):
-        _lib.check(_lib.lib.lbswim_ensemble_step(self._h, int(nsteps)))
+    def Step(self, nsteps=1, limits=None):
+        """nsteps batched steps; with `limits` (one int per member, in
+        membership order) member m takes only the first limits[m] of them."""
+        if limits is None:
+            _lib.check(_lib.lib.lbswim_ensemble_step(self._h, int(nsteps)))
+            return
+        if len(limits) != len(self._members):
+            raise ValueError("one limit per member")
+        arr = (C.c_int * max(1, len(limits)))(*[int(x) for x in limits])
+        _lib.check(_lib.lib.lbswim_ensemble_step_limited(self._h, int(nsteps), arr))
 
     def autotune(self):
         """Pick the faster slab shape per lattice shape (timed on scratch copies)."""

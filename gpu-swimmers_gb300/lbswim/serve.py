@@ -314,11 +314,14 @@ class Server:
                 if self.autotune:
                     self.ens.autotune()
                 members_changed = False
-            k = min(self.chunk, min(j.remaining for j in active))
-            self.ens.Step(k)
-            for j in active:
-                j.remaining -= k
-                updates += j.spec.sites * k
+            # a full chunk for the batch; a solve that needs fewer steps takes
+            # only those and leaves at the chunk's end
+            k = min(self.chunk, max(j.remaining for j in active))
+            lim = [min(k, j.remaining) for j in active]
+            self.ens.Step(k, limits=lim)
+            for j, kj in zip(active, lim):
+                j.remaining -= kj
+                updates += j.spec.sites * kj
             finished = [j for j in active if j.remaining <= 0]
             if finished:
                 active = [j for j in active if j.remaining > 0]

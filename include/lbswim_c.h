@@ -93,12 +93,10 @@ extern "C" {
 /* FP32/BF16/FP16 lattices with nz a multiple of 32 and the 8 x 32 slab shape:
  * the step kernel bulk-copies whole rows of distributions into shared memory
  * (cp.async.bulk, completed on an mbarrier) instead of loading them thread by
- * thread, and an FP32 lattice stepped by lbswim_system_step with one swimmer
- * array also interpolates u(t+1) at the swimmers' dipole ends in the step
- * kernel, which the swimmer move then takes.  The results are the same bits.
- * Off by default: on GB300 the two-stage copy pipeline that fits beside the
- * spreading state (two CTAs per SM) keeps too few bytes in flight, and the
- * step ran slower (0.81 ms against 0.55 ms at 256^3, 1.05 ms with the gather). */
+ * thread.  The results are the same bits.  Off by default: on GB300 the
+ * two-stage copy pipeline that fits beside the spreading state (two CTAs per
+ * SM) keeps too few bytes in flight, and the step kernel ran slower (0.81 ms
+ * against 0.55 ms at 256^3). */
 #define LBSWIM_COMPAT_BULK_COPY 32
 
 /* ---- sticky status bits (lbswim_lattice_get_status) ----------------------- */
@@ -336,6 +334,11 @@ int lbswim_ensemble_set_members(lbswim_ensemble* ens, lbswim_lattice* const* lat
                                 lbswim_swimmers* const* swimmers, lbswim_tracers* const* tracers,
                                 int n);
 int lbswim_ensemble_step(lbswim_ensemble* ens, int nsteps);
+/* nsteps batched steps in which member m takes only the first limits[m] (a
+ * member whose solve ends within the run stops there while the others go on;
+ * limits[m] <= 0 leaves it as it is).  limits holds one int per member, in
+ * set_members order; NULL is lbswim_ensemble_step. */
+int lbswim_ensemble_step_limited(lbswim_ensemble* ens, int nsteps, const int* limits);
 int lbswim_ensemble_autotune(lbswim_ensemble* ens);
 /* Slab shape of a lattice's step kernel: 0 = 8 x 32 cross-section, 1 = 16 x 16. */
 int lbswim_lattice_get_tile(const lbswim_lattice* lat, int* tile);

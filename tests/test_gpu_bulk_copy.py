@@ -1,8 +1,6 @@
 """The step kernel's bulk-copied rows (cp.async.bulk into shared memory, with
 LBSWIM_COMPAT_BULK_COPY when nz is a multiple of 32) give the same bits as its
-per-thread loads, and its interpolation of u(t+1) at the swimmers' dipole ends
-(the system step of an FP32 lattice with that flag) the same bits as the
-swimmer move's own gather from the velocity field.
+per-thread loads.
 
 Same workload twice, one lattice with the flag: after system steps with
 pending forces, steps from a materialised dense force, and ragged slabs in x

@@ -80,8 +80,9 @@ class _FakeEnsemble:
     def autotune(self):
         pass
 
-    def Step(self, k):
+    def Step(self, k, limits=None):
         assert self.members
+        assert limits is None or (len(limits) == len(self.members) and max(limits) <= k)
         self.steps += k
         if self.delay:
             time.sleep(self.delay)
