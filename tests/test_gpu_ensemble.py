@@ -147,3 +147,22 @@ def test_member_swimmer_limit():
             else:
                 with pytest.raises(_lib.LbswimError, match="32767 swimmers"):
                     ens.set_members([(lat, sw)])
+
+
+def test_members_with_step_limits_stop_where_their_own_steps_end():
+    # a run of 9 batched steps in which members take 9, 4, 0, 7 and 1 of them:
+    # each ends exactly where its own System.Step of that many steps ends,
+    # and one that took none is untouched
+    from lbswim.ensemble import Ensemble
+    batched, alone = _build(SPECS), _build(SPECS)
+    for b, a in zip(batched, alone):
+        a[0].tile = b[0].tile
+    limits = [9, 4, 0, 7, 1]
+    ens = Ensemble([(lat, sw, tr) for lat, sw, tr, _ in batched])
+    ens.Step(9, limits=limits)
+    ens.Step(3)  # then everyone goes on together
+    for a, n in zip(alone, limits):
+        a[3].Step(n + 3)
+    for b, a, n in zip(batched, alone, limits):
+        assert b[0].time_step == a[0].time_step == n + 3
+        _same(b, a)
