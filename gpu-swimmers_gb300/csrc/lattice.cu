@@ -508,6 +508,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
   if (active) load(wrap_once(x0 - 1, nx));
 
   float Fp0 = 0.f, Fp1 = 0.f, Fp2 = 0.f;
+  float nonfinite = 0.f;  // stays 0 while every output density is finite
   // this site's post-collision populations 0 (plane k-1) and 1 (planes k-1, k-2)
   float keep0 = 0.f, keep1a = 0.f, keep1b = 0.f;
   int k3 = 0;  // k % 3
@@ -582,7 +583,9 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
       }
       float R, jx, jy, jz;
       hydro_moments(g, R, jx, jy, jz);
-      if (!finite_f(R + jx + jy + jz)) raise_status(a.status, LBSWIM_STATUS_NONFINITE);
+      // 0 * R is 0 for a finite R and NaN otherwise; a non-finite population
+      // makes R non-finite (it is their sum)
+      nonfinite = __fmaf_rn(0.f, R, nonfinite);
       S* __restrict__ fn = (S*)a.f_new;
       S* __restrict__ bo = fn + fidx<S, I>(0, s, N);
 #pragma unroll
@@ -602,6 +605,7 @@ __device__ __forceinline__ void fused_slab(const FusedArgs& a, int tz, int ty, i
     keep1a = new1;
     k3 = k3 == 2 ? 0 : k3 + 1;
   }
+  if (nonfinite != 0.f) raise_status(a.status, LBSWIM_STATUS_NONFINITE);
 }
 
 template <class S, int TZ, int TY, bool SPREAD, class I, bool TMA>

@@ -860,8 +860,10 @@ __device__ __forceinline__ double q44_to_pos(long long q) {
 }
 
 // r + v moved back into [0, n) by one shift, like wrap_position<float>: in Q44
-// when r and r + v allow it, else in FP64.
-__device__ __forceinline__ double advance_position(double r, float v, int n) {
+// when r and r + v allow it (the result then lies in the box by construction),
+// else in FP64, where a result outside [0, n) -- a non-finite r or v, or a
+// move longer than the box -- raises LBSWIM_STATUS_PARTICLE_OUTSIDE.
+__device__ __forceinline__ double advance_position(double r, float v, int n, unsigned* status) {
   long long q;
   if (n < (1 << 19) && fabsf(v) < (float)n && pos_to_q44(r, q)) {
     q += fx_quant(v, 0x1.0p44f);
@@ -869,7 +871,9 @@ __device__ __forceinline__ double advance_position(double r, float v, int n) {
     q = q >= nq ? q - nq : (q < 0 ? q + nq : q);
     return q44_to_pos(q);
   }
-  return wrap_position<float>(r + f2d_exact(v), n);
+  const double out = wrap_position<float>(r + f2d_exact(v), n);
+  if (!in_box(out, n)) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
+  return out;
 }
 
 // The 53-bit uniform of rng_normal3 rounded to FP32 (relative error 2^-24 at
@@ -1032,10 +1036,8 @@ __device__ __forceinline__ void tracers_move_block(int blk, int ntr, double* __r
   for (int d = 0; d < 3; ++d) {
     const double vd = f2d_exact(vv[d]);
     v[(long long)ntr * d + i] = vd;
-    const double rn = advance_position(rr[d], vv[d], D.n[d]);
-    r[(long long)ntr * d + i] = rn;
+    r[(long long)ntr * d + i] = advance_position(rr[d], vv[d], D.n[d], status);
     s[(long long)ntr * d + i] = ss[d] + vd;
-    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
   }
 }
 
@@ -1069,9 +1071,7 @@ __device__ __forceinline__ void swimmer_update(int i, int nsw, double* __restric
     float rDot = mP * (float)nd[d];
     if (!c.translational_advection_off) rDot += v[d];
     swv[nsw * d + i] = f2d_exact(rDot);
-    const double rn = advance_position(r[d], rDot, D.n[d]);
-    swr[nsw * d + i] = rn;
-    if (!in_box(rn, D.n[d])) raise_status(status, LBSWIM_STATUS_PARTICLE_OUTSIDE);
+    swr[nsw * d + i] = advance_position(r[d], rDot, D.n[d], status);
   }
   if (tumble) {
     float nn[3];
