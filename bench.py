@@ -576,7 +576,7 @@ def ensemble_arm(args, world=1, rank=0):
             "speedup_vs_plain_f64": batched / plain,
             "u_rel_l2_vs_f64": err, "u_check_members": len(chk) * world,
             "tiles": {"8x32": tiles.count(0), "16x16": tiles.count(1)},
-            "launches_per_step": 4, "graph": "two steps captured, replayed"}
+            "launches_per_step": 5, "graph": "two steps captured, replayed"}
 
 
 def serving_arm(args, world=1, rank=0):

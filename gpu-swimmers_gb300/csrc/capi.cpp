@@ -51,15 +51,6 @@ using namespace lbswim;
 
 static void check_lattice(const void* lat) { REQUIRE(lat, "lattice handle is NULL"); }
 
-// Uploaded particle positions and orientations must be finite: a NaN or an
-// infinity would otherwise travel through the moves' stencil arithmetic.  The
-// scan has no early exit so that it vectorises (it runs at memory speed).
-static void require_finite(const double* a, size_t n, const char* what) {
-  unsigned bad = 0;
-  for (size_t i = 0; i < n; ++i) bad |= !(std::fabs(a[i]) <= 1.7976931348623157e308);
-  if (bad) throw LbswimError{LBSWIM_EINVAL, std::string(what) + " holds a non-finite value"};
-}
-
 extern "C" {
 
 const char* lbswim_last_error(void) { return g_err.c_str(); }
@@ -370,6 +361,8 @@ int lbswim_swimmers_destroy(lbswim_swimmers* sw) {
   cudaFree(W->r);
   cudaFree(W->v);
   cudaFree(W->nv);
+  if (W->stage) cudaFree(W->stage);
+  if (W->flag) cudaFree(W->flag);
   if (W->done) cudaEventDestroy(W->done);
   if (W->recorded) cudaEventDestroy(W->recorded);
   if (W->copy) cudaStreamDestroy(W->copy);
@@ -424,15 +417,29 @@ int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host) {
   API_BEGIN
   REQUIRE(sw && host, "NULL argument");
   Swimmers* W = SW(sw);
-  if (field == LBSWIM_SW_R || field == LBSWIM_SW_N)
-    require_finite(host, 3 * (size_t)W->n,
-                   field == LBSWIM_SW_R ? "swimmer positions" : "swimmer orientations");
+  const size_t bytes = sizeof(double) * 3 * W->n;
+  // positions and orientations must be finite: checked on a staged copy
+  // before the field changes
+  const bool check = (field == LBSWIM_SW_R || field == LBSWIM_SW_N) && W->n > 0;
+  if (check) {
+    if (!W->stage) {
+      LB_CUDA(cudaMalloc(&W->stage, bytes));
+      LB_CUDA(cudaMalloc(&W->flag, 256));
+    }
+    upload_checked_finite(W->stage, host, 3LL * W->n, W->flag,
+                          field == LBSWIM_SW_R ? "swimmer positions" : "swimmer orientations");
+  }
   // the arrays are not bound to one stream: wait for the last kernel that used
   // them (on whichever stream), not for the whole device, and for the end
   // records a system step made of them after its move
   swimmers_wait(W);
   if (W->recorded) LB_CUDA(cudaEventSynchronize(W->recorded));
-  LB_CUDA(cudaMemcpy(sw_field(W, field), host, sizeof(double) * 3 * W->n, cudaMemcpyHostToDevice));
+  if (check) {
+    LB_CUDA(cudaMemcpyAsync(sw_field(W, field), W->stage, bytes, cudaMemcpyDeviceToDevice, 0));
+    LB_CUDA(cudaStreamSynchronize(0));
+  } else {
+    LB_CUDA(cudaMemcpy(sw_field(W, field), host, bytes, cudaMemcpyHostToDevice));
+  }
   API_END
 }
 
@@ -559,7 +566,6 @@ int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host) {
   API_BEGIN
   REQUIRE(tr && host, "NULL argument");
   REQUIRE(field >= LBSWIM_TR_R && field <= LBSWIM_TR_V, "unknown tracer field");
-  if (field == LBSWIM_TR_R) require_finite(host, 3 * (size_t)TR(tr)->n, "tracer positions");
   tracers_h2d(TR(tr), field, host);
   API_END
 }

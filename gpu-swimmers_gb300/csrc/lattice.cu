@@ -264,6 +264,43 @@ __global__ void k_packed_to_f64(const float* __restrict__ packed, double* __rest
   }
 }
 
+// The same conversions one site per thread, for a page-locked host buffer that
+// the kernel reads or writes itself (no staging copy): rho as rho - rho0 in
+// .w, u's three components [3][N] into .xyz.
+__global__ void k_rho_from_host(const double* __restrict__ src, float4* __restrict__ packed,
+                                long long N, double rho0) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    packed[i].w = (float)(src[i] - rho0);
+}
+__global__ void k_u_from_host(const double* __restrict__ src, float4* __restrict__ packed,
+                              long long N) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    float4 p = packed[i];
+    p.x = (float)src[i];
+    p.y = (float)src[N + i];
+    p.z = (float)src[2 * N + i];
+    packed[i] = p;
+  }
+}
+__global__ void k_rho_to_host(const float4* __restrict__ packed, double* __restrict__ dst,
+                              long long N, double rho0) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (double)packed[i].w + rho0;
+}
+__global__ void k_u_to_host(const float4* __restrict__ packed, double* __restrict__ dst,
+                            long long N) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float4 p = packed[i];
+    dst[i] = p.x;
+    dst[N + i] = p.y;
+    dst[2 * N + i] = p.z;
+  }
+}
+
 // Host FP64 <-> device storage conversions for H2D / D2H of fOld and fNew:
 // host element e of the reference's [15][N] order is population e / N at site
 // e % N, stored at fidx.
@@ -841,6 +878,21 @@ static double* staging(Lattice* L, size_t elems) {
   return L->staging;
 }
 
+// Page-locked host memory (cudaMallocHost, cudaHostRegister, pinned tensors)
+// is mapped into the device's address space, so a conversion kernel can read
+// or write the caller's buffer itself over the host link: one pass, with no
+// staging copy and no serialisation of copy and conversion.  Returns the
+// buffer's device address, or null for pageable memory (which goes through
+// the staging buffer).
+static const void* mapped_host(const void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 void lattice_zero_force_now(Lattice* L) {
   const size_t he = L->precision == LBSWIM_F64 ? 8 : 4;
   LB_CUDA(cudaMemsetAsync(L->force, 0, 3 * L->n * he, L->stream));
@@ -880,11 +932,16 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sums(const S* __restrict__ f,
                                                       double rho0, double* __restrict__ part) {
   __shared__ double red[4][SUM_THREADS];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (long long s = blockIdx.x * (long long)SUM_THREADS + threadIdx.x; s < N;
-       s += (long long)SUM_BLOCKS * SUM_THREADS) {
-    if (hydro) {
-      acc[0] += (double)hydro[s].w;
-    } else {
+  if (hydro) {
+    // several loads in flight per thread; the adds keep their order
+    const float* rw = reinterpret_cast<const float*>(hydro) + 3;
+#pragma unroll 8
+    for (long long s = blockIdx.x * (long long)SUM_THREADS + threadIdx.x; s < N;
+         s += (long long)SUM_BLOCKS * SUM_THREADS)
+      acc[0] += (double)__ldg(rw + 4 * s);
+  } else {
+    for (long long s = blockIdx.x * (long long)SUM_THREADS + threadIdx.x; s < N;
+         s += (long long)SUM_BLOCKS * SUM_THREADS) {
       double m = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
 #pragma unroll
       for (int p = 0; p < 15; ++p) {
@@ -912,11 +969,20 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sums(const S* __restrict__ f,
     for (int q = 0; q < 4; ++q) part[blockIdx.x * 4 + q] = red[q][0];
 }
 
-__global__ void k_sums_final(const double* __restrict__ part, double* __restrict__ out) {
-  double t[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int b = 0; b < SUM_BLOCKS; ++b)
-    for (int q = 0; q < 4; ++q) t[q] += part[b * 4 + q];
-  for (int q = 0; q < 4; ++q) out[q] = t[q];
+// The block sums are staged in shared memory by the whole block; then one
+// thread per quantity adds them in block order (a chain of 512 dependent adds
+// that no longer waits on a global load each).
+constexpr int SUM_FINAL_THREADS = 512;
+__global__ void __launch_bounds__(SUM_FINAL_THREADS) k_sums_final(const double* __restrict__ part,
+                                                                  double* __restrict__ out) {
+  __shared__ double sp[SUM_BLOCKS * 4];
+  for (int i = threadIdx.x; i < SUM_BLOCKS * 4; i += SUM_FINAL_THREADS) sp[i] = part[i];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int b = 0; b < SUM_BLOCKS; ++b) t += sp[b * 4 + threadIdx.x];
+    out[threadIdx.x] = t;
+  }
 }
 
 // out = {sum (rho - rho0), 0, 0, 0} from the packed velocity buffer, or
@@ -926,7 +992,7 @@ static void sums_t(Lattice* L, bool from_hydro, double out[4]) {
   double* part = staging(L, SUM_BLOCKS * 4 + 4);
   k_sums<S><<<SUM_BLOCKS, SUM_THREADS, 0, L->stream>>>(
       (const S*)L->f[L->cur], from_hydro ? L->hydro : nullptr, L->n, L->rho0, part);
-  k_sums_final<<<1, 1, 0, L->stream>>>(part, part + SUM_BLOCKS * 4);
+  k_sums_final<<<1, SUM_FINAL_THREADS, 0, L->stream>>>(part, part + SUM_BLOCKS * 4);
   LB_CHECK_LAUNCH(2);
   LB_CUDA(cudaMemcpyAsync(out, part + SUM_BLOCKS * 4, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                           L->stream));
@@ -1183,6 +1249,12 @@ static long long field_count(const Lattice* L, int field) {
 template <class S>
 static void f_h2d_t(Lattice* L, void* dst, const double* host) {
   const long long total = 15 * L->n;
+  if (const double* mh = (const double*)mapped_host(host)) {
+    k_f_from_f64<S><<<grid_for(total, 256), 256, 0, L->stream>>>(mh, (S*)dst, 0, total, L->n,
+                                                                  L->rho0);
+    LB_CHECK_LAUNCH(1);
+    return;
+  }
   const long long chunk = std::min<long long>(total, 1LL << 24);
   double* st = staging(L, chunk);
   for (long long off = 0; off < total; off += chunk) {
@@ -1198,6 +1270,13 @@ static void f_h2d_t(Lattice* L, void* dst, const double* host) {
 template <class S>
 static void f_d2h_t(Lattice* L, const void* src, double* host) {
   const long long total = 15 * L->n;
+  if (double* mh = (double*)mapped_host(host)) {
+    k_f_to_f64<S><<<grid_for(total, 256), 256, 0, L->stream>>>((const S*)src, mh, 0, total,
+                                                                L->n, L->rho0);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaStreamSynchronize(L->stream));
+    return;
+  }
   const long long chunk = std::min<long long>(total, 1LL << 24);
   double* st = staging(L, chunk);
   for (long long off = 0; off < total; off += chunk) {
@@ -1242,6 +1321,15 @@ void lattice_h2d(Lattice* L, int field, const double* host) {
       case LBSWIM_BF16: f_h2d_t<__nv_bfloat16>(L, dst, host); break;
       default: f_h2d_t<__half>(L, dst, host); break;
     }
+  } else if (const double* mh = (const double*)mapped_host(host)) {
+    const long long N = L->n;
+    if (field == LBSWIM_FIELD_FORCE)
+      k_f64_to_f32<<<grid_for(cnt, 256), 256, 0, L->stream>>>(mh, (float*)dst, cnt);
+    else if (field == LBSWIM_FIELD_RHO)
+      k_rho_from_host<<<grid_for(N, 256), 256, 0, L->stream>>>(mh, L->hydro, N, L->rho0);
+    else
+      k_u_from_host<<<grid_for(N, 256), 256, 0, L->stream>>>(mh, L->hydro, N);
+    LB_CHECK_LAUNCH(1);
   } else {
     const long long chunk = std::min<long long>(cnt, 1LL << 24);
     double* st = staging(L, chunk);
@@ -1275,6 +1363,18 @@ void lattice_d2h(Lattice* L, int field, double* host) {
       case LBSWIM_BF16: f_d2h_t<__nv_bfloat16>(L, src, host); break;
       default: f_d2h_t<__half>(L, src, host); break;
     }
+    return;
+  }
+  if (double* mh = (double*)mapped_host(host)) {
+    const long long N = L->n;
+    if (field == LBSWIM_FIELD_FORCE)
+      k_f32_to_f64<<<grid_for(cnt, 256), 256, 0, L->stream>>>((const float*)src, mh, cnt);
+    else if (field == LBSWIM_FIELD_RHO)
+      k_rho_to_host<<<grid_for(N, 256), 256, 0, L->stream>>>(L->hydro, mh, N, L->rho0);
+    else
+      k_u_to_host<<<grid_for(N, 256), 256, 0, L->stream>>>(L->hydro, mh, N);
+    LB_CHECK_LAUNCH(1);
+    LB_CUDA(cudaStreamSynchronize(L->stream));
     return;
   }
   const long long chunk = std::min<long long>(cnt, 1LL << 24);

@@ -166,6 +166,8 @@ struct Swimmers {
   // for its next step (they read r and n after the move): uploads wait for it
   cudaEvent_t recorded = nullptr;
   cudaStream_t copy = nullptr;  // host copies of several fields in one wait
+  double* stage = nullptr;      // [3][n] upload checked before it replaces a field
+  unsigned* flag = nullptr;     // result of the upload check
 };
 
 // Tracers live on the device in a work order binned by position (8^3-site
@@ -185,6 +187,7 @@ struct Tracers {
   int* perm2 = nullptr;
   int* bin_of = nullptr;
   double* staging = nullptr;  // [3][n] user order, for H2D / D2H
+  unsigned* flag = nullptr;   // result of the upload check
   bool identity = true;       // perm is the identity
   bool needs_sort = true;
   int moves_since_sort = 0;
@@ -325,6 +328,11 @@ void tracers_move_async(Tracers* T, Lattice* L);
 void tracers_alloc(Tracers* T);
 void tracers_free(Tracers* T);
 void tracers_h2d(Tracers* T, int field, const double* host);
+// Upload of n doubles into the device buffer `stage`, then a check on the
+// device that they are all finite (LbswimError LBSWIM_EINVAL naming `what`
+// otherwise).  Legacy default stream; returns once the check is read.
+void upload_checked_finite(double* stage, const double* host, long long n, unsigned* flag,
+                           const char* what);
 void tracers_d2h(Tracers* T, int field, double* host);
 void lattice_interp_velocity(Lattice* L, int npoints, const double* r_host, double* v_host);
 void lattice_init_random(Lattice* L, unsigned long long seed, double amp);

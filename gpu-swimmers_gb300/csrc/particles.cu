@@ -1692,6 +1692,32 @@ __global__ void k_tr_reorder(int n, const int* __restrict__ perm, const double* 
   }
 }
 
+// Any non-finite value among n doubles sets *flag.
+__global__ void k_any_nonfinite(const double* __restrict__ a, long long n,
+                                unsigned* __restrict__ flag) {
+  unsigned bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    bad |= !(fabs(a[i]) <= 1.7976931348623157e308);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// The check runs on the device, on the uploaded copy: a host scan of the
+// caller's buffer by one core reads it several times slower than the link
+// delivers it (1M tracer positions: ~1.2 ms against 0.12 ms for the copy).
+void upload_checked_finite(double* stage, const double* host, long long n, unsigned* flag,
+                           const char* what) {
+  if (n <= 0) return;
+  LB_CUDA(cudaMemcpy(stage, host, sizeof(double) * n, cudaMemcpyHostToDevice));
+  LB_CUDA(cudaMemset(flag, 0, sizeof(unsigned)));
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 8);
+  k_any_nonfinite<<<(int)blocks, 256>>>(stage, n, flag);
+  LB_CHECK_LAUNCH(1);
+  unsigned bad = 0;
+  LB_CUDA(cudaMemcpy(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (bad) throw LbswimError{LBSWIM_EINVAL, std::string(what) + " holds a non-finite value"};
+}
+
 void tracers_alloc(Tracers* T) {
   const size_t n = (size_t)(T->n > 0 ? T->n : 1);
   double** bufs[] = {&T->r, &T->s, &T->v, &T->r2, &T->s2, &T->v2, &T->staging};
@@ -1702,6 +1728,7 @@ void tracers_alloc(Tracers* T) {
   LB_CUDA(cudaMalloc(&T->perm, sizeof(int) * n));
   LB_CUDA(cudaMalloc(&T->perm2, sizeof(int) * n));
   LB_CUDA(cudaMalloc(&T->bin_of, sizeof(int) * n));
+  LB_CUDA(cudaMalloc(&T->flag, 256));
   k_iota<<<(int)((n + 255) / 256), 256>>>((int)n, T->perm);
   LB_CHECK_LAUNCH(1);
   LB_CUDA(cudaDeviceSynchronize());
@@ -1716,7 +1743,7 @@ void tracers_free(Tracers* T) {
   }
   void* ptrs[] = {T->r,    T->s,      T->v,      T->r2,        T->s2,        T->v2,
                   T->perm, T->perm2,  T->bin_of, T->staging,   T->bin_count, T->bin_start,
-                  T->scan_tmp};
+                  T->scan_tmp, T->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -1729,10 +1756,21 @@ void tracers_h2d(Tracers* T, int field, const double* host) {
   LB_CUDA(cudaDeviceSynchronize());  // particle arrays are not bound to one stream
   if (T->n <= 0) return;
   double* dst = tr_field_ptr(T, field);
+  const size_t bytes = sizeof(double) * 3 * T->n;
+  // positions must be finite: checked on the staged copy, before the field
+  // changes
+  const bool check = field == LBSWIM_TR_R;
+  if (check)
+    upload_checked_finite(T->staging, host, 3LL * T->n, T->flag, "tracer positions");
   if (T->identity) {
-    LB_CUDA(cudaMemcpy(dst, host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+    if (check) {
+      LB_CUDA(cudaMemcpyAsync(dst, T->staging, bytes, cudaMemcpyDeviceToDevice, 0));
+      LB_CUDA(cudaStreamSynchronize(0));
+    } else {
+      LB_CUDA(cudaMemcpy(dst, host, bytes, cudaMemcpyHostToDevice));
+    }
   } else {
-    LB_CUDA(cudaMemcpy(T->staging, host, sizeof(double) * 3 * T->n, cudaMemcpyHostToDevice));
+    if (!check) LB_CUDA(cudaMemcpy(T->staging, host, bytes, cudaMemcpyHostToDevice));
     k_tr_reorder<true><<<(T->n + 255) / 256, 256>>>(T->n, T->perm, T->staging, dst);
     LB_CHECK_LAUNCH(1);
     LB_CUDA(cudaDeviceSynchronize());

@@ -230,7 +230,8 @@ int lbswim_swimmers_add_forces(lbswim_swimmers* sw, lbswim_lattice* lat);
 /* SwimmerArray::Move, SwimmerArray.cu:212-220. */
 int lbswim_swimmers_move(lbswim_swimmers* sw, lbswim_lattice* lat);
 /* SharedArray<double>::H2D / D2H of r, v or n (3*n doubles).  Positions and
- * orientations must be finite (else LBSWIM_EINVAL, nothing copied). */
+ * orientations must be finite (else LBSWIM_EINVAL and the field keeps its
+ * values; the check runs on the device, on a staged copy). */
 int lbswim_swimmers_h2d(lbswim_swimmers* sw, int field, const double* host);
 int lbswim_swimmers_d2h(lbswim_swimmers* sw, int field, double* host);
 /* No reference counterpart: the D2H of r, v and n (any may be NULL) with one
@@ -294,7 +295,8 @@ int lbswim_tracers_destroy(lbswim_tracers* tr);
 int lbswim_tracers_get_num(const lbswim_tracers* tr, int* out);
 /* TracerArray::Move, TracerArray.cu:45-52. */
 int lbswim_tracers_move(lbswim_tracers* tr, lbswim_lattice* lat);
-/* Positions must be finite (else LBSWIM_EINVAL, nothing copied). */
+/* Positions must be finite (else LBSWIM_EINVAL and the field keeps its values;
+ * the check runs on the device, on a staged copy). */
 int lbswim_tracers_h2d(lbswim_tracers* tr, int field, const double* host);
 int lbswim_tracers_d2h(lbswim_tracers* tr, int field, double* host);
 

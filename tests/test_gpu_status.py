@@ -4,7 +4,8 @@ validation of uploads.
 A non-finite density is uploaded (plain arithmetic on a finite-size field, no
 bad index anywhere): the step and CalcHydro kernels flag it, the status stays
 set until read with clear, and a healthy lattice reports nothing.  Particle
-uploads with a NaN or an infinity are rejected before any copy.
+uploads with a NaN or an infinity are rejected (checked on the device, on a
+staged copy) and leave the field as it was.
 """
 import numpy as np
 import pytest
@@ -55,8 +56,11 @@ def test_nonfinite_particle_uploads_are_rejected():
     assert np.array_equal(sw.r.data, before)  # nothing was copied
     tr = tracers.Array(7)
     tr.r[:] = 2.0
+    tr.r.H2D()
     tr.r[0, 3] = np.nan
     with pytest.raises(_lib.LbswimError, match="non-finite"):
         tr.r.H2D()
+    tr.r.D2H()
+    assert np.all(tr.r.data == 2.0)  # nothing was copied
     tr.v[:] = np.nan  # velocities are outputs of the move; not checked
     tr.v.H2D()
