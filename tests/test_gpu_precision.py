@@ -79,16 +79,19 @@ def _spread_case():
     return O.random_case((40, 24, 36), 400, 300, seed=21, alpha=0.1, P=2e-3, l=0.4)
 
 
-@pytest.mark.parametrize("kind", ["sparse", "dense", "folded"])
+@pytest.mark.parametrize("kind", ["sparse", "dense", "ragged", "folded"])
 def test_f32_in_kernel_spread_equals_materialised_force(kind):
     # (a) the step kernel spreads the pending ends itself; (b) the force is read
     # back first, which writes the dense field, and the step then reads it.
-    # The dense case puts more ends on one slab and one plane than the kernel's
-    # shared-memory lists hold, which exercises its fallbacks; the folded case
-    # also takes the 64-bit sums with carries.
+    # The dense case puts more ends on one slab and one plane than the kernels'
+    # shared-memory lists hold, which exercises their fallbacks; the ragged case
+    # has partial slabs and tiles on every axis; the folded case also takes
+    # the 64-bit sums with carries.
     case = {"sparse": _spread_case,
             "dense": lambda: O.random_case((16, 16, 16), 600, 50, seed=3, alpha=0.1, P=2e-3,
                                            l=0.4),
+            "ragged": lambda: O.random_case((17, 9, 33), 120, 40, seed=9, alpha=0.1, P=2e-3,
+                                            l=0.4),
             "folded": lambda: O.random_case((3, 8, 12), 2100, 10, seed=5, alpha=0.1, P=2e-3,
                                             l=0.4)}[kind]()
     a = build_gpu(case, "f32")
