@@ -174,10 +174,13 @@ __global__ void k_calc_hydro(const S* __restrict__ f, const H* __restrict__ F, H
     T fx, fy, fz;
     load_force(F, N, s, fx, fy, fz);
     const T r = rho0 + R;
+    // one division per site (GB300's FP64 pipe is narrow; within an ulp of
+    // the reference's three, lb.cu:286-293)
+    const T inv = T(1) / r;
     rho[s] = r;
-    u[s] = (jx + T(0.5) * fx) / r;
-    u[N + s] = (jy + T(0.5) * fy) / r;
-    u[2 * N + s] = (jz + T(0.5) * fz) / r;
+    u[s] = (jx + T(0.5) * fx) * inv;
+    u[N + s] = (jy + T(0.5) * fy) * inv;
+    u[2 * N + s] = (jz + T(0.5) * fz) * inv;
     if (!finite_d((double)(r + jx + jy + jz))) raise_status(status, LBSWIM_STATUS_NONFINITE);
   }
 }

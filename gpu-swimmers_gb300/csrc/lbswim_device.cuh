@@ -514,6 +514,15 @@ __device__ __forceinline__ T axis_weight(int x, int o, int n, const T phi[4]) {
 }
 
 // Does the stencil of an end with origin o cover coordinate x on an axis of n
+// sites?  (With n < 4 its four nodes cover every coordinate.)
+__device__ __forceinline__ bool covers_axis(int x, int o, int n) {
+  if (n < 4) return true;
+  int d = x - o;
+  if (d < 0) d += n;
+  return d <= 3;
+}
+
+// Does the stencil of an end with origin o cover coordinate x on an axis of n
 // sites, and with which summed weight (n < 4 folds several nodes onto x)?
 template <class T>
 __device__ __forceinline__ bool cover_weight(int x, int o, int n, const T phi[4], T& w) {

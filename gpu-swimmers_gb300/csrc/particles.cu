@@ -496,6 +496,8 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
   auto rec = [&](int q) -> const EndRecord<T>& { return in_smem ? srec[q] : ends[sorted[s0 + q]]; };
   const int z = kz * FT_Z + lane;
   const bool zval = z < D.n[2];
+  // no axis shorter than a stencil: one node of an end lands on a site
+  const bool single = D.n[0] >= 4 && D.n[1] >= 4 && D.n[2] >= 4;
   for (int row = warp; row < FT_X * FT_Y; row += FT_THREADS / 32) {
     const int x = kx * FT_X + (row >> 3), y = ky * FT_Y + (row & 7);
     if (x >= D.n[0] || y >= D.n[1]) continue;
@@ -514,18 +516,31 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
       bool covers = false;
       if (q < cnt) {
         const EndRecord<T>& e = rec(q);
-        T w;
-        covers = cover_weight(x, e.o[0], D.n[0], e.phi[0], w) &&
-                 cover_weight(y, e.o[1], D.n[1], e.phi[1], w);
+        covers = covers_axis(x, e.o[0], D.n[0]) && covers_axis(y, e.o[1], D.n[1]);
       }
-      unsigned m = __ballot_sync(0xffffffffu, covers);
-      while (m) {
-        const int q2i = base + __ffs(m) - 1;
-        m &= m - 1;
-        const EndRecord<T>& e = rec(q2i);
-        T wz;
-        if (!zval || !cover_weight(z, e.o[2], D.n[2], e.phi[2], wz)) continue;
-        hit = true;
+      // this lane's ends among those covering the row (they also cover its z),
+      // in end order; each lane then adds its own, so that the FP64 work of
+      // the row's ends runs on all the lanes they cover at once
+      const unsigned m = __ballot_sync(0xffffffffu, covers);  // every lane takes part
+      unsigned mine = 0u;
+      if (zval)
+        for (unsigned mm = m; mm; mm &= mm - 1) {
+          const int b = __ffs(mm) - 1;
+          if (covers_axis(z, rec(base + b).o[2], D.n[2])) mine |= 1u << b;
+        }
+      hit |= mine != 0u;
+      for (; mine; mine &= mine - 1) {
+        const EndRecord<T>& e = rec(base + __ffs(mine) - 1);
+        if (single) {
+          int i = x - e.o[0], j = y - e.o[1], k = z - e.o[2];
+          i += i < 0 ? D.n[0] : 0;
+          j += j < 0 ? D.n[1] : 0;
+          k += k < 0 ? D.n[2] : 0;
+          acc0 = __dadd_rn(acc0, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[0]));
+          acc1 = __dadd_rn(acc1, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[1]));
+          acc2 = __dadd_rn(acc2, end_contrib(e.phi[0][i], e.phi[1][j], e.phi[2][k], e.F[2]));
+          continue;
+        }
         // node by node in (i, j, k) order, as AccumulateDeltaForce adds them
         // (several nodes land on one site when an axis is shorter than 4)
         for (int i = 0; i < 4; ++i) {
