@@ -246,6 +246,18 @@ __device__ __forceinline__ void peskin_weights4(float dr, float w[4]) {
   w[3] = 0.125f * (q - s);
 }
 
+// The same four weights in FP64 (the default FP64 particle moves; exact mode
+// keeps the reference's delta per node, below).
+__device__ __forceinline__ void peskin_weights4(double dr, double w[4]) {
+  const double a = dr - 1.0;
+  const double s = sqrt(fma(4.0 * a, 1.0 - a, 1.0));
+  const double p = 3.0 - 2.0 * a, q = 1.0 + 2.0 * a;
+  w[0] = 0.125 * (p - s);
+  w[1] = 0.125 * (p + s);
+  w[2] = 0.125 * (q + s);
+  w[3] = 0.125 * (q - s);
+}
+
 // FP64: the reference's operations in its order, each rounded on its own (no
 // fused multiply-add), so that FP64 lattices can reproduce the oracle bit for bit.
 template <>

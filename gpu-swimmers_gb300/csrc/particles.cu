@@ -566,24 +566,25 @@ __global__ void __launch_bounds__(FT_THREADS) k_force_tile(Dims D, TileGrid G,
 }
 
 // ---- Move kernels -----------------------------------------------------------
-// Stencil nodes and Peskin weights of position r (interp.cu:23-30).  The FP64
-// path keeps the reference's arithmetic; the FP32 path takes one FP64
-// difference per axis and forms the four arguments in FP32 (GB300's FP64 pipe
-// is narrow).
-template <class T>
+// Stencil nodes and Peskin weights of position r (interp.cu:23-30).  FP64
+// lattices in exact mode keep the reference's arithmetic (a delta per node);
+// the default FP64 moves (FAST) take the four weights of an axis from one
+// square root; the FP32 path takes one FP64 difference per axis and forms the
+// four arguments in FP32 (GB300's FP64 pipe is narrow).
+template <class T, bool FAST = false>
 __device__ __forceinline__ void interp_setup(const Dims& D, const double r[3], int idx[3][4],
                                              T phi[3][4]) {
   for (int d = 0; d < 3; ++d) {
     const double x0 = ceil(r[d] - 2.);
     const int o = wrap_any((int)x0, D.n[d]);
-    float w[4];
-    if constexpr (sizeof(T) == 4) peskin_weights4((float)(r[d] - x0), w);
+    T w[4];
+    if constexpr (sizeof(T) == 4 || FAST) peskin_weights4((T)(r[d] - x0), w);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int t = o + i;
       while (t >= D.n[d]) t -= D.n[d];
       idx[d][i] = t;
-      if constexpr (sizeof(T) == 8)
+      if constexpr (sizeof(T) == 8 && !FAST)
         phi[d][i] = peskin_delta<T>(r[d] - (x0 + i));
       else
         phi[d][i] = w[i];
@@ -604,13 +605,14 @@ __device__ __forceinline__ double wrap_position(double r, int n) {
 }
 
 // InterpVelocity, interp.cu:8-47: u at r through the 4^3 Peskin stencil, from
-// the FP64 SoA field ...
-template <class T>
+// the FP64 SoA field (FAST: fused multiply-adds and one square root per axis,
+// the default FP64 moves) ...
+template <class T, bool FAST = false>
 __device__ __forceinline__ void interp_velocity(const double* __restrict__ u, const Dims& D,
                                                 const double r[3], T v[3]) {
   int idx[3][4];
   T phi[3][4];
-  interp_setup<T>(D, r, idx, phi);
+  interp_setup<T, FAST>(D, r, idx, phi);
   v[0] = v[1] = v[2] = T(0);
   const long long nynz = (long long)D.n[1] * D.n[2];
   for (int i = 0; i < 4; ++i)
@@ -621,9 +623,15 @@ __device__ __forceinline__ void interp_velocity(const double* __restrict__ u, co
       for (int k = 0; k < 4; ++k) {
         const T d3 = pij * phi[2][k];
         const long long s = row + idx[2][k];
-        v[0] = add_prod(v[0], d3, (T)u[s]);
-        v[1] = add_prod(v[1], d3, (T)u[D.N + s]);
-        v[2] = add_prod(v[2], d3, (T)u[2 * D.N + s]);
+        if constexpr (FAST) {
+          v[0] = fma(d3, (T)u[s], v[0]);
+          v[1] = fma(d3, (T)u[D.N + s], v[1]);
+          v[2] = fma(d3, (T)u[2 * D.N + s], v[2]);
+        } else {
+          v[0] = add_prod(v[0], d3, (T)u[s]);
+          v[1] = add_prod(v[1], d3, (T)u[D.N + s]);
+          v[2] = add_prod(v[2], d3, (T)u[2 * D.N + s]);
+        }
       }
     }
 }
@@ -653,8 +661,9 @@ __device__ __forceinline__ void interp_velocity(const float4* __restrict__ h, co
     }
 }
 
-// DoSwimmerArrayMove, SwimmerArray.cu:123-210.
-template <class U, class T>
+// DoSwimmerArrayMove, SwimmerArray.cu:123-210 (FAST: the default FP64
+// interpolation of interp_velocity).
+template <class U, class T, bool FAST = false>
 __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __restrict__ swv,
                                 double* __restrict__ swn, lbswim_common_params c,
                                 unsigned long long seed, unsigned long long step, Dims D,
@@ -667,7 +676,7 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     n0[d] = swn[nsw * d + i];
   }
   T v[3];
-  interp_velocity<T>(u, D, r, v);
+  interp_velocity<T, FAST>(u, D, r, v);
   double rMinus[3];
   for (int d = 0; d < 3; ++d) {
     double rDot = __dmul_rn(__dmul_rn(c.mobility, c.P), n0[d]);
@@ -684,7 +693,7 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
     rng_normal3(seed, (uint32_t)i, step, nn);
   } else if (!c.rotational_advection_off) {  // rotate with the local shear
     T vm[3];
-    interp_velocity<T>(u, D, rMinus, vm);
+    interp_velocity<T, FAST>(u, D, rMinus, vm);
     for (int d = 0; d < 3; ++d) nn[d] = n0[d] + ((double)v[d] - (double)vm[d]) / c.l;
   } else {
     return;  // orientation unchanged
@@ -694,8 +703,9 @@ __global__ void k_swimmers_move(int nsw, double* __restrict__ swr, double* __res
   for (int d = 0; d < 3; ++d) swn[nsw * d + i] = nn[d] / norm;
 }
 
-// DoTracerArrayMove, TracerArray.cu:12-43 (s accumulated per tracer).
-template <class U, class T>
+// DoTracerArrayMove, TracerArray.cu:12-43 (s accumulated per tracer; FAST: the
+// default FP64 interpolation of interp_velocity).
+template <class U, class T, bool FAST = false>
 __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restrict__ s,
                                double* __restrict__ v, Dims D, const U* __restrict__ u,
                                unsigned* status) {
@@ -707,7 +717,7 @@ __global__ void k_tracers_move(int ntr, double* __restrict__ r, double* __restri
     ss[d] = s[ntr * d + i];
   }
   T vv[3];
-  interp_velocity<T>(u, D, rr, vv);
+  interp_velocity<T, FAST>(u, D, rr, vv);
   for (int d = 0; d < 3; ++d) {
     const double vd = (double)vv[d];
     v[ntr * d + i] = vd;
@@ -1554,8 +1564,12 @@ void swimmers_move(Swimmers* W, Lattice* L) {
   const Dims D = make_dims(L);
   if (W->n > 0) {
     const int grid = (W->n + 255) / 256;
-    if (L->precision == LBSWIM_F64)
+    if (L->precision == LBSWIM_F64 && (L->compat & LBSWIM_COMPAT_EXACT_F64))
       k_swimmers_move<double, double><<<grid, 256, 0, L->stream>>>(
+          W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u,
+          L->status);
+    else if (L->precision == LBSWIM_F64)
+      k_swimmers_move<double, double, true><<<grid, 256, 0, L->stream>>>(
           W->n, W->r, W->v, W->nv, W->common, W->seed, W->step, D, (const double*)L->u,
           L->status);
     else if (wide_particle_index(L))
@@ -1847,9 +1861,12 @@ static void tracers_move_on(Tracers* T, Lattice* L, cudaStream_t stream) {
   T->moves_since_sort++;
   const Dims D = make_dims(L);
   const int grid = (T->n + 255) / 256;
-  if (L->precision == LBSWIM_F64)
+  if (L->precision == LBSWIM_F64 && (L->compat & LBSWIM_COMPAT_EXACT_F64))
     k_tracers_move<double, double><<<grid, 256, 0, stream>>>(T->n, T->r, T->s, T->v, D,
                                                                  (const double*)L->u, L->status);
+  else if (L->precision == LBSWIM_F64)
+    k_tracers_move<double, double, true><<<grid, 256, 0, stream>>>(
+        T->n, T->r, T->s, T->v, D, (const double*)L->u, L->status);
   else if (wide_particle_index(L))
     k_tracers_move_f32<long long><<<(T->n + TRACER_MOVE_BLOCK - 1) / TRACER_MOVE_BLOCK,
                                     TRACER_MOVE_BLOCK, 0, stream>>>(T->n, T->r, T->s, T->v, D,
