@@ -3,8 +3,8 @@
 With LBSWIM_COMPAT_EXACT_F64 every FP64 array is the oracle's, bit for bit,
 and hashes to the digest that the reference's own host build wrote into the
 fixture.  The default FP64 path (butterfly moment transform and fused
-multiply-adds in the lattice kernels; the particle kernels keep the
-reference's order) is held to:
+multiply-adds in the lattice kernels; one square root per axis for the Peskin
+weights and fused multiply-adds in the particle moves) is held to:
   rho, f        relative L2 <= 1e-12;
   u, force, v   relative L2 normalised by the field's max magnitude <= 1e-10
                 (u is a small difference of O(0.1) sums, 1e-8..1e-5 here, so
