@@ -889,11 +889,14 @@ static double* staging(Lattice* L, size_t elems) {
 // the staging buffer).
 static const void* mapped_host(const void* host) {
   cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+  int dev = -1;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) {
     (void)cudaGetLastError();
     return nullptr;
   }
-  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+  // page-locked by this device's context (memory pinned under another
+  // device takes the staging path)
+  return at.type == cudaMemoryTypeHost && at.device == dev ? at.devicePointer : nullptr;
 }
 
 void lattice_zero_force_now(Lattice* L) {
