@@ -63,49 +63,6 @@ def test_noalloc_spread_matches_add_forces_twice():
     assert rel_l2_maxnorm(force.cpu().numpy().reshape(3, N), 2 * expected) <= TOL_F64
 
 
-def test_noalloc_spread_captured_in_a_cuda_graph():
-    # after a first call on the device (it looks up the scratch array's
-    # address), a call is captured into a CUDA graph; each replay overwrites
-    # the caller's force buffer with the spread
-    torch = pytest.importorskip("torch")
-    from lbswim import _lib
-    shape = (16, 12, 20)
-    N = int(np.prod(shape))
-    case = O.random_case(shape, 200, 0, seed=17, P=2e-3, l=0.4)
-    lat, sw, _, _ = build_gpu(case, "f64")
-    lat.ZeroForce()
-    sw.AddForces(lat)
-    lat.force.D2H()
-    expected = lat.force.data.reshape(3, N).copy()
-    s = case["swimmers"]
-    r = _dev(torch, s["r"])
-    n = _dev(torch, s["nvec"])
-    force = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
-    side = torch.cuda.Stream()
-
-    def call():
-        return _lib.lib.lbswim_spread_forces_noalloc(
-            C.c_void_p(r.data_ptr()), C.c_void_p(n.data_ptr()), s["n"], s["P"], s["l"],
-            shape[0], shape[1], shape[2], C.c_void_p(force.data_ptr()), 0,
-            C.c_void_p(side.cuda_stream))
-
-    torch.cuda.synchronize()
-    with torch.cuda.stream(side):
-        _lib.check(call())
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph, stream=side):
-        rc = call()
-    _lib.check(rc)
-    for _ in range(2):
-        force.fill_(-7.0)
-        torch.cuda.synchronize()
-        graph.replay()
-        torch.cuda.synchronize()
-        got = force.cpu().numpy().reshape(3, N)
-        assert rel_l2_maxnorm(got, expected) <= TOL_F64
-
-
 def test_noalloc_spread_rejects_sizes_beyond_its_limit():
     torch = pytest.importorskip("torch")
     from lbswim import _lib
