@@ -299,14 +299,15 @@ int lbswim_lattice_device_ptr(const lbswim_lattice* lat, int field, void** ptr, 
 }
 
 int lbswim_lattice_set_timing(lbswim_lattice* lat, int enable) {
-  API_BEGIN
+  // events around the step kernel change nothing a prepared step depends on
+  API_BEGIN_READ
   check_lattice(lat);
   LAT(lat)->timing = enable != 0;
   API_END
 }
 
 int lbswim_lattice_get_timing(lbswim_lattice* lat, double* total_ms, int* launches) {
-  API_BEGIN
+  API_BEGIN_READ
   check_lattice(lat);
   REQUIRE(total_ms && launches, "NULL argument");
   lattice_read_timing(LAT(lat), total_ms, launches);

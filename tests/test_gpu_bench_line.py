@@ -41,6 +41,7 @@ def test_bench_prints_the_contract_line():
     assert roof["bound"] == "hbm" and roof["unit"] == "GB/s" and roof["peak"] > 0
     assert abs(roof["frac"] - roof["achieved"] / roof["peak"]) <= 1e-9
     assert 0 < roof["frac"] < 1.5 and roof["kernel"] == "k_fused_step"
+    assert roof["timed_launches"].startswith("1 of %d" % steps)  # every 4th of 4 steps
     e2e = d["e2e"]
     assert e2e["unit"] == "GLUPS" and 0 < e2e["value"] < d["value"]
     assert e2e["h2d_bytes_per_step"] > 0 and e2e["d2h_bytes_per_step"] > 0
